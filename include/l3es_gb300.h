@@ -1,0 +1,109 @@
+/*
+ * l3es_gb300 — C ABI of the GB300 (sm_103a) pseudo-spectral DNS hot path.
+ *
+ * Drop-in boundary for the l3es call surface (tumaer/ql-les-data). The reference
+ * is a Python/JAX package of closures; each entry point below replaces one of its
+ * functions, cited as file:line inside that project. Host code (the Python drop-in
+ * package, or any C/C++/ctypes caller) passes raw CUDA device pointers, sizes and a
+ * cudaStream_t (as void*). No PyTorch or CUDA-runtime types appear in signatures.
+ *
+ * Conventions
+ *   - Spectral fields use the reference layout: 3D u_hat (batch, 3, N, N, N/2+1),
+ *     2D u_hat (batch, 3, N, N/2+1), complex64 (interleaved float re, im), i.e. the
+ *     output of jnp.fft.rfftn(u, axes) (l3es/spectral_solver.py:206).
+ *   - Physical fields are float32 (batch, 3, N, N, N) in 3D, (batch, 3, N, N, 1) in 2D.
+ *   - Every call is asynchronous on `stream` and returns 0 or a negative L3ES_E*
+ *     code; it never aborts the process. l3es_last_error() describes the last
+ *     failure of the calling thread.
+ *   - A plan is not re-entrant: use one plan per stream. The plan owns its
+ *     twiddle tables and scratch memory (allocated in l3es_plan_create); arrays
+ *     passed to the calls are owned by the caller.
+ */
+#ifndef L3ES_GB300_H
+#define L3ES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define L3ES_OK 0
+#define L3ES_EINVAL (-1)   /* bad argument (size, pointer, mode) */
+#define L3ES_ECUDA (-2)    /* CUDA runtime error (launch, allocation) */
+#define L3ES_ENOMEM (-3)   /* device allocation failed */
+#define L3ES_ESTATE (-4)   /* call not valid for this plan */
+
+#define L3ES_FORCING_NONE 0        /* forcing_type="none" */
+#define L3ES_FORCING_EKIN_TOT 1    /* forcing_type="ekin_tot" (spectral_solver.py:82-112) */
+#define L3ES_FORCING_CONST_POWER 2 /* extension: eps/(2 E_f) u_hat on 0<|k|^2<=kf^2 */
+
+typedef struct l3es_plan l3es_plan;
+
+/* Solver parameters of set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf,
+ * e_kin_target, forcing_type) (l3es/spectral_solver.py:156-168) that the step needs. */
+typedef struct l3es_plan_desc {
+  int32_t dim;        /* 2 or 3 (fft_axes (1,2) or (1,2,3)) */
+  int32_t n;          /* grid points per axis: 16, 32, 64, 128, 256 or 512 */
+  int32_t batch;      /* independent trajectories stepped together (reference: 1) */
+  int32_t forcing;    /* L3ES_FORCING_* */
+  int32_t kf;         /* forcing band 0 < |k|^2 <= kf^2 (init_fields.py:167-188) */
+  int32_t kolm_k;     /* extension, 2D: f_x = kolm_amp sin(kolm_k y); 0 = off */
+  double nu;          /* viscosity */
+  double dt;          /* time step */
+  double e_kin_init;  /* ekin_tot target E0 (spectral_solver.py:209), all trajectories */
+  double eps_inj;     /* extension: constant-power injection rate */
+  double drag;        /* extension: linear drag coefficient */
+  double kolm_amp;    /* extension: Kolmogorov forcing amplitude */
+} l3es_plan_desc;
+
+/* Builds the closures' constant state of rhs_wrapper / rk4_wrapper
+ * (l3es/spectral_solver.py:27-48, :65-71): twiddle tables, dealias band, scratch. */
+int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out);
+
+/* Releases the plan's device memory. */
+int l3es_plan_destroy(l3es_plan* plan);
+
+/* Per-trajectory ekin_tot target E0 (host array of `batch` doubles);
+ * the reference computes it once in set_up_solver (spectral_solver.py:209). */
+int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count);
+
+/* Scratch bytes the plan holds on the device (for capacity planning). */
+int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
+
+/* nsteps calls of step_fn(u, u_hat) (l3es/spectral_solver.py:73-118), in place on
+ * u_hat. u_out (nullable) receives irfftn(u_hat) after the last step (:114-116).
+ * e_inj_dev (nullable, device, nsteps*batch doubles) receives the per-step
+ * injection rate of ekin_tot forcing (:109), 0 otherwise.
+ * The first RK stage evaluates u from u_hat instead of reading the caller's u;
+ * irfftn(rfftn(u)) == u for real u, so the result is the same up to rounding. */
+int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
+              double* e_inj_dev, void* stream);
+
+/* rhs_fn(u, u_hat, rk) (l3es/spectral_solver.py:50-60): du = P[dealias *
+ * rfftn(u x curl u)] - nu k^2 u_hat (+ enabled extension terms), u from u_hat.
+ * du: device, same shape as u_hat, must not alias it. */
+int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream);
+
+/* jnp.fft.rfftn(u, axes=fft_axes) of a real field (spectral_solver.py:206). */
+int l3es_rfftn(l3es_plan* plan, const float* u, void* u_hat, void* stream);
+
+/* jnp.fft.irfftn(u_hat, axes=fft_axes) (spectral_solver.py:52, :114). */
+int l3es_irfftn(l3es_plan* plan, const void* u_hat, float* u, void* stream);
+
+/* Kinetic energy 0.5 mean(sum u^2) of irfftn(u_hat), by Parseval in FP64
+ * (spectral_solver.py:318, :94). out_dev: device, batch doubles. */
+int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, void* stream);
+
+/* Last error message of the calling thread ("" if none). */
+const char* l3es_last_error(void);
+
+/* Library version string. */
+const char* l3es_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* L3ES_GB300_H */

@@ -1,0 +1,217 @@
+// Register/shared-memory FFT building blocks for sm_103a.
+//
+// An N-point complex FFT is computed cooperatively by T = N/E threads of a CTA,
+// each holding E = 8 complex values in registers. The algorithm is Stockham
+// autosort (Govindaraju et al., SC'08): radix-R stages (R <= E), E/R butterflies
+// per thread and stage, data exchanged through shared memory between stages.
+// Input element n and output element k both live in thread n % T, slot n / T,
+// so a forward FFT can consume the register output of an inverse FFT directly.
+//
+// Twiddles come from a table tw[m] = exp(-2 pi i m / Ntab) computed in FP64 on the
+// host and stored FP32; an N-point FFT indexes it with stride Ntab / N.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace l3es {
+
+constexpr int kFwd = -1;  // exp(-i ...): numpy fft / rfft
+constexpr int kInv = +1;  // exp(+i ...): numpy ifft / irfft (unnormalised)
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+// multiply by exp(DIR * i * pi / 2): DIR=-1 -> -i, DIR=+1 -> +i
+template <int DIR>
+__device__ __forceinline__ float2 mul_i(float2 a) {
+  return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+// twiddle from the FP32 table, conjugated for the inverse direction
+template <int DIR>
+__device__ __forceinline__ float2 twid(const float2* __restrict__ tw, int idx) {
+  float2 w = __ldg(tw + idx);
+  return DIR < 0 ? w : conjf2(w);
+}
+
+// cos/sin(2 pi k / 16), k = 0..3 (first quadrant), exact decimal constants
+__device__ __forceinline__ float c16(int k) {
+  return k == 0 ? 1.0f : k == 1 ? 0.92387953251128674f : k == 2 ? 0.70710678118654752f : 0.38268343236508978f;
+}
+
+// In-register DFT of size R (2, 4, 8, 16), natural order in and out.
+template <int R, int DIR>
+struct Dft;
+
+template <int DIR>
+struct Dft<1, DIR> {
+  static __device__ __forceinline__ void run(float2*) {}
+};
+
+template <int DIR>
+struct Dft<2, DIR> {
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <int DIR>
+struct Dft<4, DIR> {
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    float2 s13 = cadd(v[1], v[3]), d13 = mul_i<DIR>(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+  }
+};
+
+// radix-2 decimation in time on top of two half-size DFTs
+template <int R, int DIR>
+struct DftSplit {
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 e[R / 2], o[R / 2];
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) {
+      e[i] = v[2 * i];
+      o[i] = v[2 * i + 1];
+    }
+    Dft<R / 2, DIR>::run(e);
+    Dft<R / 2, DIR>::run(o);
+#pragma unroll
+    for (int k = 0; k < R / 2; ++k) {
+      float2 t;
+      // W_R^k = exp(DIR * 2 pi i k / R) expressed in sixteenths of a turn
+      const int q = k * (16 / R);  // 0..7
+      if (q == 0) {
+        t = o[k];
+      } else if (q == 4) {
+        t = mul_i<DIR>(o[k]);
+      } else {
+        // angle 2 pi q / 16 in (0, pi): cos = c16(q) (q<4) or -c16(8-q) ...
+        float cr, si;
+        if (q < 4) {
+          cr = c16(q);
+          si = c16(4 - q);
+        } else {
+          cr = -c16(8 - q);
+          si = c16(q - 4);
+        }
+        const float2 w = make_float2(cr, DIR * si);
+        t = cmul(o[k], w);
+      }
+      v[k] = cadd(e[k], t);
+      v[k + R / 2] = csub(e[k], t);
+    }
+  }
+};
+
+template <int DIR>
+struct Dft<8, DIR> {
+  static __device__ __forceinline__ void run(float2* v) { DftSplit<8, DIR>::run(v); }
+};
+template <int DIR>
+struct Dft<16, DIR> {
+  static __device__ __forceinline__ void run(float2* v) { DftSplit<16, DIR>::run(v); }
+};
+
+// Compile-time stage schedule: radix E until the remainder is smaller than E.
+template <int N, int E>
+struct Sched {
+  static constexpr int ilog(int n, int e) { return n < e ? 0 : 1 + ilog(n / e, e); }
+  static constexpr int ipow(int e, int k) { return k == 0 ? 1 : e * ipow(e, k - 1); }
+  static constexpr int kFull = ilog(N, E);           // number of radix-E stages
+  static constexpr int kRem = N / ipow(E, kFull);    // last radix (1 if none)
+  static constexpr int kStages = kFull + (kRem > 1 ? 1 : 0);
+  static constexpr int radix(int s) { return s < kFull ? E : kRem; }
+  static constexpr int ns(int s) { return ipow(E, s); }  // Ns before stage s
+};
+
+// Padded exchange index: one spare slot every 8 elements keeps the radix-8 strided
+// writes of the first stage on distinct shared-memory banks. A buffer for n
+// elements holds xpad_len(n) slots.
+__device__ __forceinline__ int xpad(int n) { return n + (n >> 3); }
+__host__ __device__ constexpr int xpad_len(int n) { return n + n / 8; }
+
+// One Stockham stage. FIRST: inputs from registers; LAST: outputs to registers.
+// sm: exchange buffer, element n at sm[xpad(n) * SS].
+template <int N, int E, int R, int NS, int DIR, int SS, bool FIRST, bool LAST>
+__device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t,
+                                               const float2* __restrict__ tw, int tws) {
+  constexpr int T = N / E;
+  constexpr int BPT = E / R;  // butterflies per thread
+  float2 x[BPT][R];
+#pragma unroll
+  for (int b = 0; b < BPT; ++b) {
+    const int j = t + T * b;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      x[b][r] = FIRST ? v[b + r * BPT] : sm[xpad(j + r * (N / R)) * SS];
+    }
+  }
+  if (!FIRST && !LAST) __syncthreads();  // all reads done before the in-place writes
+#pragma unroll
+  for (int b = 0; b < BPT; ++b) {
+    const int j = t + T * b;
+    if (NS > 1) {
+      const int jm = j % NS;
+#pragma unroll
+      for (int r = 1; r < R; ++r) x[b][r] = cmul(x[b][r], twid<DIR>(tw, r * jm * (N / (NS * R)) * tws));
+    }
+    Dft<R, DIR>::run(x[b]);
+    if (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[b + r * BPT] = x[b][r];
+    } else {
+      const int base = (j / NS) * NS * R + (j % NS);
+#pragma unroll
+      for (int r = 0; r < R; ++r) sm[xpad(base + r * NS) * SS] = x[b][r];
+    }
+  }
+  if (!LAST) __syncthreads();
+}
+
+template <int N, int E, int DIR, int SS, int S, bool DONE = (S >= Sched<N, E>::kStages)>
+struct Stages;
+template <int N, int E, int DIR, int SS, int S>
+struct Stages<N, E, DIR, SS, S, false> {
+  using Sc = Sched<N, E>;
+  static __device__ __forceinline__ void run(float2 (&v)[E], float2* sm, int t,
+                                             const float2* __restrict__ tw, int tws) {
+    stockham_stage<N, E, Sc::radix(S), Sc::ns(S), DIR, SS, S == 0, S == Sc::kStages - 1>(v, sm, t, tw, tws);
+    Stages<N, E, DIR, SS, S + 1>::run(v, sm, t, tw, tws);
+  }
+};
+template <int N, int E, int DIR, int SS, int S>
+struct Stages<N, E, DIR, SS, S, true> {
+  static __device__ __forceinline__ void run(float2 (&)[E], float2*, int, const float2* __restrict__, int) {}
+};
+
+// N-point FFT by T = N/E threads; every thread of the CTA must call it (it contains
+// __syncthreads). v[e] holds element t + T*e on entry and on exit. tws: stride into
+// the twiddle table (table length / N). The exchange buffer is free on return
+// only after the caller's next __syncthreads.
+template <int N, int E, int DIR, int SS>
+__device__ __forceinline__ void block_fft(float2 (&v)[E], float2* sm, int t,
+                                          const float2* __restrict__ tw, int tws) {
+  Stages<N, E, DIR, SS, 0>::run(v, sm, t, tw, tws);
+}
+
+// Elements per thread used for an N-point FFT.
+template <int N>
+struct Fft {
+  static constexpr int E = N >= 8 ? 8 : N;
+  static constexpr int T = N / E;
+};
+
+// signed integer wavenumber of FFT index i on a full axis of length n (fftfreq)
+__device__ __forceinline__ int kfull(int i, int n) { return i < n / 2 ? i : i - n; }
+
+}  // namespace l3es

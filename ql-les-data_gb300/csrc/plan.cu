@@ -1,0 +1,305 @@
+// Plan management and the C ABI of the DNS step (include/l3es_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "l3es_internal.h"
+
+struct l3es_plan {
+  l3es_plan_desc desc;
+  l3es::Ctx ctx;
+  l3es::DnsTable tab;
+  int device = 0;
+  long long ws_bytes = 0;
+  std::vector<void*> allocs;
+};
+
+namespace l3es {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return L3ES_OK;
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return L3ES_ECUDA;
+}
+
+bool dns_table(int n, DnsTable* out) {
+  switch (n) {
+    case 16: *out = make_dns_table<16>(); return true;
+    case 32: *out = make_dns_table<32>(); return true;
+    case 64: *out = make_dns_table<64>(); return true;
+    case 128: *out = make_dns_table<128>(); return true;
+    case 256: *out = make_dns_table<256>(); return true;
+    case 512: *out = make_dns_table<512>(); return true;
+    default: return false;
+  }
+}
+
+// Largest |k| kept by the cube mask |k_i| < 2/3 (N/2+1) (spectral_solver.py:42-48),
+// with the reference's float64 comparison.
+static int dealias_kd(int n) {
+  const double kmax = 2.0 / 3.0 * (double)(n / 2 + 1);
+  int kd = 0;
+  while ((double)(kd + 1) < kmax) ++kd;
+  return kd;
+}
+
+// FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n)
+static std::vector<float2> twiddles(int n) {
+  std::vector<float2> t(n);
+  const double pi = 3.14159265358979323846;
+  for (int m = 0; m < n; ++m) {
+    const double a = -2.0 * pi * (double)m / (double)n;
+    t[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  return t;
+}
+
+// Parseval kinetic energy: per-block partial sums of w |u_hat|^2 over 3 components.
+__global__ void __launch_bounds__(256)
+k_energy_partial(const float2* __restrict__ uh, long long cs, int h, int nblk, double* __restrict__ partial) {
+  const int batch = blockIdx.y;
+  const float2* ub = uh + (long long)batch * 3 * cs;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cs; i += (long long)nblk * blockDim.x) {
+    const int kh = (int)(i % h);
+    const double w = (kh == 0 || kh == h - 1) ? 1.0 : 2.0;
+    double a = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      const float2 v = ub[c * cs + i];
+      a += (double)v.x * v.x + (double)v.y * v.y;
+    }
+    s += w * a;
+  }
+  block_sum_store(s, partial, batch * nblk + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256)
+k_sum_partials(const double* __restrict__ partial, int n, double scale, double* __restrict__ out) {
+  __shared__ double red[32];
+  const int batch = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[(long long)batch * n + i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+    out[batch] = t * scale;
+  }
+}
+
+}  // namespace l3es
+
+using namespace l3es;
+
+#define L3ES_TRY_CUDA(expr, what)                          \
+  do {                                                     \
+    int _rc = cuda_check((expr), (what));                  \
+    if (_rc != L3ES_OK) return _rc;                        \
+  } while (0)
+
+static int plan_alloc(l3es_plan* p, void** ptr, size_t bytes, const char* what) {
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(L3ES_ENOMEM, std::string("cudaMalloc(") + what + ", " + std::to_string(bytes) +
+                                 " B): " + cudaGetErrorString(e));
+  }
+  p->allocs.push_back(*ptr);
+  p->ws_bytes += (long long)bytes;
+  return L3ES_OK;
+}
+
+static void plan_free(l3es_plan* p) {
+  for (void* a : p->allocs) cudaFree(a);
+  p->allocs.clear();
+}
+
+extern "C" {
+
+const char* l3es_last_error(void) { return g_err.c_str(); }
+
+const char* l3es_version(void) { return "l3es_gb300 0.1 (sm_103a)"; }
+
+int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
+  if (!desc || !out) return fail(L3ES_EINVAL, "l3es_plan_create: null argument");
+  *out = nullptr;
+  const int n = desc->n, dim = desc->dim;
+  if (dim != 2 && dim != 3) return fail(L3ES_EINVAL, "dim must be 2 or 3, got " + std::to_string(dim));
+  DnsTable tab;
+  if (!dns_table(n, &tab))
+    return fail(L3ES_EINVAL, "N=" + std::to_string(n) + " not supported (16, 32, 64, 128, 256, 512)");
+  if (desc->batch < 1) return fail(L3ES_EINVAL, "batch must be >= 1");
+  if (!(desc->dt > 0.0) || !(desc->nu >= 0.0)) return fail(L3ES_EINVAL, "need dt > 0 and nu >= 0");
+  if (desc->forcing < L3ES_FORCING_NONE || desc->forcing > L3ES_FORCING_CONST_POWER)
+    return fail(L3ES_EINVAL, "unknown forcing mode " + std::to_string(desc->forcing));
+  if (desc->forcing != L3ES_FORCING_NONE && (desc->kf < 1 || desc->kf > n / 4))
+    return fail(L3ES_EINVAL, "forcing needs 1 <= kf <= N/4");
+  if (desc->kolm_k != 0 && (dim != 2 || desc->kolm_k < 0 || desc->kolm_k >= n / 2))
+    return fail(L3ES_EINVAL, "Kolmogorov forcing is 2D with 0 < kolm_k < N/2");
+
+  auto* p = new l3es_plan();
+  p->desc = *desc;
+  cudaGetDevice(&p->device);
+  Ctx& c = p->ctx;
+  c.dim = dim;
+  c.n = n;
+  c.h = n / 2 + 1;
+  c.batch = desc->batch;
+  c.kd = dealias_kd(n);
+  c.kt = ((c.kd + 1 + TW - 1) / TW) * TW;
+  c.nmid = dim == 3 ? n : 1;
+  c.cs = c.nmid * n * c.h;
+  c.fs = c.cs;
+  c.ds = c.nmid * n * c.kt;
+  c.ps = dim == 3 ? (long long)n * n * n : (long long)n * n;
+  c.npartial = ((c.h + TW - 1) / TW) * (int)c.nmid;
+  c.kf = desc->kf;
+  c.eps_inj = desc->eps_inj;
+  p->tab = tab;
+
+  const size_t B = (size_t)c.batch;
+  int rc = L3ES_OK;
+  rc = rc ? rc : plan_alloc(p, (void**)&c.tw, sizeof(float2) * n, "twiddles");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.W, sizeof(float2) * B * 6 * c.fs, "W");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.DU, sizeof(float2) * B * 3 * c.ds, "DU");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.Tb, sizeof(float2) * B * 3 * c.cs, "stage");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.C, sizeof(float2) * B * 3 * c.cs, "accumulator");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.partial, sizeof(double) * B * c.npartial, "partials");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.band, sizeof(double) * B, "band");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.e0, sizeof(double) * B, "e0");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");
+  if (rc != L3ES_OK) {
+    plan_free(p);
+    delete p;
+    return rc;
+  }
+  std::vector<float2> tw = twiddles(n);
+  std::vector<double> e0(B, desc->e_kin_init);
+  cudaError_t e = cudaMemcpy(c.tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    rc = cuda_check(e, "l3es_plan_create");
+    plan_free(p);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return L3ES_OK;
+}
+
+int l3es_plan_destroy(l3es_plan* plan) {
+  if (!plan) return L3ES_OK;
+  plan_free(plan);
+  delete plan;
+  return L3ES_OK;
+}
+
+int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count) {
+  if (!plan || !e0_host) return fail(L3ES_EINVAL, "l3es_plan_set_e0: null argument");
+  if (count != plan->ctx.batch) return fail(L3ES_EINVAL, "l3es_plan_set_e0: count != batch");
+  return cuda_check(cudaMemcpy(plan->ctx.e0, e0_host, sizeof(double) * count, cudaMemcpyHostToDevice),
+                    "l3es_plan_set_e0");
+}
+
+int64_t l3es_plan_workspace_bytes(const l3es_plan* plan) { return plan ? plan->ws_bytes : 0; }
+
+int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, void* stream) {
+  if (!plan || !u_hat) return fail(L3ES_EINVAL, "l3es_step: null plan or u_hat");
+  if (nsteps < 0) return fail(L3ES_EINVAL, "l3es_step: nsteps < 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  const Ctx& c = plan->ctx;
+  const l3es_plan_desc& d = plan->desc;
+  float2* S = (float2*)u_hat;
+  static const double a_rk4[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+  static const double b_rk4[3] = {0.5, 0.5, 1.0};
+  const double inv_n2d = 1.0 / std::pow((double)c.n, 2 * c.dim);
+  const double eps64 = 2.220446049250313e-16;  // jnp.finfo(float).eps, spectral_solver.py:23
+  for (int st = 0; st < nsteps; ++st) {
+    for (int rk = 0; rk < 4; ++rk) {
+      EpiParams prm;
+      prm.a_dt = (float)(a_rk4[rk] * d.dt);
+      prm.b_dt = rk < 3 ? (float)(b_rk4[rk] * d.dt) : 0.f;
+      prm.nu = (float)d.nu;
+      prm.drag = (float)d.drag;
+      prm.kolm_amp = (float)d.kolm_amp;
+      prm.kolm_k = d.kolm_k;
+      prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
+      prm.rk = rk;
+      prm.want_energy = (d.forcing == L3ES_FORCING_EKIN_TOT && rk == 3) ? 1 : 0;
+      plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
+    }
+    double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
+    if (d.forcing == L3ES_FORCING_EKIN_TOT) {
+      if (c.dim == 3)
+        k_force_ekin<3><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf, inv_n2d,
+                                                eps64, einj, nullptr);
+      else
+        k_force_ekin<2><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf, inv_n2d,
+                                                eps64, einj, nullptr);
+    } else if (e_inj_dev) {
+      L3ES_TRY_CUDA(cudaMemsetAsync(einj, 0, sizeof(double) * c.batch, s), "l3es_step memset");
+    }
+  }
+  if (u_out) plan->tab.irfftn(c, S, u_out, s);
+  return cuda_check(cudaGetLastError(), "l3es_step launch");
+}
+
+int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream) {
+  if (!plan || !u_hat || !du) return fail(L3ES_EINVAL, "l3es_rhs: null argument");
+  if (u_hat == du) return fail(L3ES_EINVAL, "l3es_rhs: du must not alias u_hat");
+  const l3es_plan_desc& d = plan->desc;
+  EpiParams prm;
+  prm.a_dt = 0.f;
+  prm.b_dt = 0.f;
+  prm.nu = (float)d.nu;
+  prm.drag = (float)d.drag;
+  prm.kolm_amp = (float)d.kolm_amp;
+  prm.kolm_k = d.kolm_k;
+  prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
+  prm.rk = -1;
+  prm.want_energy = 0;
+  plan->tab.stage(plan->ctx, (const float2*)u_hat, nullptr, (float2*)du, -1, prm, (cudaStream_t)stream);
+  return cuda_check(cudaGetLastError(), "l3es_rhs launch");
+}
+
+int l3es_rfftn(l3es_plan* plan, const float* u, void* u_hat, void* stream) {
+  if (!plan || !u || !u_hat) return fail(L3ES_EINVAL, "l3es_rfftn: null argument");
+  plan->tab.rfftn(plan->ctx, u, (float2*)u_hat, (cudaStream_t)stream);
+  return cuda_check(cudaGetLastError(), "l3es_rfftn launch");
+}
+
+int l3es_irfftn(l3es_plan* plan, const void* u_hat, float* u, void* stream) {
+  if (!plan || !u || !u_hat) return fail(L3ES_EINVAL, "l3es_irfftn: null argument");
+  plan->tab.irfftn(plan->ctx, (const float2*)u_hat, u, (cudaStream_t)stream);
+  return cuda_check(cudaGetLastError(), "l3es_irfftn launch");
+}
+
+int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, void* stream) {
+  if (!plan || !u_hat || !out_dev) return fail(L3ES_EINVAL, "l3es_kinetic_energy: null argument");
+  const Ctx& c = plan->ctx;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nblk = (int)std::min<long long>(c.npartial, (c.cs + 255) / 256);
+  k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>((const float2*)u_hat, c.cs, c.h, nblk, c.partial);
+  const double scale = 0.5 / std::pow((double)c.n, 2 * c.dim);
+  k_sum_partials<<<c.batch, 256, 0, s>>>(c.partial, nblk, scale, out_dev);
+  return cuda_check(cudaGetLastError(), "l3es_kinetic_energy launch");
+}
+
+}  // extern "C"

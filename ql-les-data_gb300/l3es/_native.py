@@ -1,0 +1,201 @@
+"""ctypes binding of the l3es_gb300 C ABI (include/l3es_gb300.h).
+
+The library is built in tree by ``ql-les-data_gb300/build.py`` (or
+``__graft_entry__.build()``). There is no fallback: if the library is missing,
+importing this module raises with the build command, and every call checks the
+returned status and raises ``RuntimeError`` with ``l3es_last_error()``.
+Tensors are torch CUDA tensors; only their device pointers cross the boundary.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libl3es_gb300.so")
+
+FORCING = {"none": 0, "ekin_tot": 1, "const_power": 2}
+
+# Every symbol declared in include/l3es_gb300.h: (restype, argtypes)
+_P = ctypes.c_void_p
+_I = ctypes.c_int32
+_SIGNATURES = {
+    "l3es_plan_create": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "l3es_plan_destroy": (ctypes.c_int, [_P]),
+    "l3es_plan_set_e0": (ctypes.c_int, [_P, _P, _I]),
+    "l3es_plan_workspace_bytes": (ctypes.c_int64, [_P]),
+    "l3es_step": (ctypes.c_int, [_P, _P, _P, _I, _P, _P]),
+    "l3es_rhs": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_rfftn": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_irfftn": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_kinetic_energy": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_last_error": (ctypes.c_char_p, []),
+    "l3es_version": (ctypes.c_char_p, []),
+}
+
+
+class PlanDesc(ctypes.Structure):
+    """l3es_plan_desc."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("n", ctypes.c_int32),
+        ("batch", ctypes.c_int32),
+        ("forcing", ctypes.c_int32),
+        ("kf", ctypes.c_int32),
+        ("kolm_k", ctypes.c_int32),
+        ("nu", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("e_kin_init", ctypes.c_double),
+        ("eps_inj", ctypes.c_double),
+        ("drag", ctypes.c_double),
+        ("kolm_amp", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the library once (raises ImportError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            f"l3es_gb300 CUDA library not found at {path}; build it with "
+            "`python ql-les-data_gb300/build.py` (nvcc, sm_103a)"
+        )
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = load().l3es_last_error().decode()
+        raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+
+def _stream(stream=None) -> int:
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _ptr(t) -> int:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("l3es_gb300 calls need CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError("l3es_gb300 calls need contiguous tensors")
+    return t.data_ptr()
+
+
+class Plan:
+    """Owns an ``l3es_plan``: twiddles, dealias band and scratch of one solver."""
+
+    def __init__(self, dim: int, n: int, nu: float, dt: float, batch: int = 1,
+                 forcing: str = "none", kf: int = 0, e_kin_init: float = 0.0,
+                 eps_inj: float = 0.0, drag: float = 0.0, kolm_k: int = 0,
+                 kolm_amp: float = 0.0):
+        lib = load()
+        if forcing not in FORCING:
+            raise ValueError(f"forcing must be one of {list(FORCING)}, got {forcing!r}")
+        self.dim, self.n, self.batch = int(dim), int(n), int(batch)
+        self.nu, self.dt = float(nu), float(dt)
+        self.forcing, self.kf = forcing, int(kf or 0)
+        d = PlanDesc(self.dim, self.n, self.batch, FORCING[forcing], self.kf, int(kolm_k),
+                     self.nu, self.dt, float(e_kin_init), float(eps_inj), float(drag),
+                     float(kolm_amp))
+        h = ctypes.c_void_p()
+        _check(lib.l3es_plan_create(ctypes.byref(d), ctypes.byref(h)), "l3es_plan_create")
+        self._h = h
+        self._lib = lib
+
+    # shapes -------------------------------------------------------------------
+    @property
+    def spec_shape(self):
+        n, h = self.n, self.n // 2 + 1
+        s = (3, n, n, h) if self.dim == 3 else (3, n, h)
+        return s if self.batch == 1 else (self.batch,) + s
+
+    @property
+    def phys_shape(self):
+        n = self.n
+        s = (3, n, n, n) if self.dim == 3 else (3, n, n, 1)
+        return s if self.batch == 1 else (self.batch,) + s
+
+    def _check_spec(self, t):
+        import torch
+
+        if t.dtype != torch.complex64 or tuple(t.shape) != self.spec_shape:
+            raise ValueError(f"expected complex64 {self.spec_shape}, got {t.dtype} {tuple(t.shape)}")
+
+    def _check_phys(self, t):
+        import torch
+
+        if t.dtype != torch.float32 or t.numel() != _prod(self.phys_shape):
+            raise ValueError(f"expected float32 {self.phys_shape}, got {t.dtype} {tuple(t.shape)}")
+
+    # calls --------------------------------------------------------------------
+    def set_e0(self, e0) -> None:
+        vals = (ctypes.c_double * self.batch)(*[float(v) for v in (e0 if hasattr(e0, "__len__") else [e0] * self.batch)])
+        _check(self._lib.l3es_plan_set_e0(self._h, vals, self.batch), "l3es_plan_set_e0")
+
+    def step(self, u_hat, nsteps: int = 1, u_out=None, e_inj=None, stream=None) -> None:
+        """In-place RK4 steps on u_hat (optionally irfftn into u_out at the end)."""
+        self._check_spec(u_hat)
+        if u_out is not None:
+            self._check_phys(u_out)
+        _check(self._lib.l3es_step(self._h, _ptr(u_hat), _ptr(u_out), int(nsteps), _ptr(e_inj),
+                                   _stream(stream)), "l3es_step")
+
+    def rhs(self, u_hat, du, stream=None) -> None:
+        self._check_spec(u_hat)
+        self._check_spec(du)
+        _check(self._lib.l3es_rhs(self._h, _ptr(u_hat), _ptr(du), _stream(stream)), "l3es_rhs")
+
+    def rfftn(self, u, u_hat, stream=None) -> None:
+        self._check_phys(u)
+        self._check_spec(u_hat)
+        _check(self._lib.l3es_rfftn(self._h, _ptr(u), _ptr(u_hat), _stream(stream)), "l3es_rfftn")
+
+    def irfftn(self, u_hat, u, stream=None) -> None:
+        self._check_spec(u_hat)
+        self._check_phys(u)
+        _check(self._lib.l3es_irfftn(self._h, _ptr(u_hat), _ptr(u), _stream(stream)), "l3es_irfftn")
+
+    def kinetic_energy(self, u_hat, out, stream=None) -> None:
+        self._check_spec(u_hat)
+        _check(self._lib.l3es_kinetic_energy(self._h, _ptr(u_hat), _ptr(out), _stream(stream)),
+               "l3es_kinetic_energy")
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self._lib.l3es_plan_workspace_bytes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.l3es_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _prod(s):
+    p = 1
+    for v in s:
+        p *= int(v)
+    return p

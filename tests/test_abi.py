@@ -1,0 +1,51 @@
+"""The C-ABI library loads and exports every symbol the public header declares."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _header_symbols():
+    src = open(os.path.join(ROOT, "include", "l3es_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(l3es_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    syms = _header_symbols()
+    for s in ("l3es_plan_create", "l3es_step", "l3es_rhs", "l3es_rfftn", "l3es_irfftn",
+              "l3es_last_error"):
+        assert s in syms
+
+
+def test_library_exports_all_header_symbols():
+    from l3es import _native
+
+    if not os.path.exists(_native.LIB_PATH):
+        pytest.skip("library not built (run __graft_entry__.build())")
+    lib = _native.load()
+    for s in _header_symbols():
+        assert hasattr(lib, s), f"{s} missing from {_native.LIB_PATH}"
+        assert s in _native._SIGNATURES, f"{s} has no ctypes signature"
+    assert lib.l3es_version().decode().startswith("l3es_gb300")
+
+
+def test_invalid_arguments_fail_without_gpu():
+    """Argument validation runs before any device work and reports a message."""
+    from l3es import _native
+
+    if not os.path.exists(_native.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _native.load()
+    h = ctypes.c_void_p()
+    d = _native.PlanDesc(dim=4, n=64, batch=1, nu=0.01, dt=0.01)
+    assert lib.l3es_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert b"dim" in lib.l3es_last_error()
+    d = _native.PlanDesc(dim=3, n=100, batch=1, nu=0.01, dt=0.01)
+    assert lib.l3es_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
+    assert b"not supported" in lib.l3es_last_error()
+    assert lib.l3es_step(None, None, None, 1, None, None) == -1

@@ -1,0 +1,153 @@
+"""CUDA DNS step vs the FP64 oracle and the reference's golden vectors (GPU).
+
+Tolerance: the CUDA path computes in FP32 (FP64 reductions); fields are compared by
+max |a - b| / max |b|, which stays below 2e-5 for the few-step cases here (FP32
+unit roundoff 6e-8 times the FFT depth and step count).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import numpy_ref as R
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+RTOL = 2e-5
+
+
+def _rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _plan(**kw):
+    from l3es import _native
+
+    return _native.Plan(**kw)
+
+
+def _c64(a):
+    return torch.from_numpy(np.ascontiguousarray(a).astype(np.complex64)).cuda()
+
+
+def _f32(a):
+    return torch.from_numpy(np.ascontiguousarray(a).astype(np.float32)).cuda()
+
+
+@pytest.mark.parametrize("dim,n", [(3, 16), (3, 32), (3, 64), (3, 128), (2, 16), (2, 64), (2, 256), (2, 512)])
+def test_rfftn_irfftn_match_numpy(dim, n):
+    rng = np.random.default_rng(n + dim)
+    shape = (3, n, n, n) if dim == 3 else (3, n, n, 1)
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    u = rng.standard_normal(shape)
+    p = _plan(dim=dim, n=n, nu=0.01, dt=0.01)
+    uh = torch.empty(p.spec_shape, dtype=torch.complex64, device="cuda")
+    p.rfftn(_f32(u), uh)
+    ref = np.fft.rfftn(u, axes=axes).reshape(p.spec_shape)
+    assert _rel(uh.cpu().numpy(), ref) < RTOL
+    # irfftn of a non-Hermitian-consistent spectrum: numpy semantics (imag of DC/Nyquist dropped)
+    spec = ref + 0.1 * (rng.standard_normal(ref.shape) + 1j * rng.standard_normal(ref.shape)) * np.abs(ref).max()
+    out = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
+    p.irfftn(_c64(spec), out)
+    ref_u = np.fft.irfftn(spec.reshape((3, n, n, n // 2 + 1) if dim == 3 else (3, n, n // 2 + 1)), axes=axes)
+    assert _rel(out.cpu().numpy().reshape(ref_u.shape), ref_u) < RTOL
+
+
+def test_rhs_matches_reference_golden(gold):
+    g = gold("rand3d_n16")
+    p = _plan(dim=3, n=16, nu=float(g["nu"]), dt=float(g["dt"]))
+    du = torch.empty(p.spec_shape, dtype=torch.complex64, device="cuda")
+    p.rhs(_c64(g["u_hat0"]), du)
+    assert _rel(du.cpu().numpy(), g["rhs_rk0"]) < RTOL
+
+
+@pytest.mark.parametrize("case", ["tgv3d_n16", "rand3d_n16"])
+def test_step3d_matches_reference_golden(gold, case):
+    g = gold(case)
+    n = int(g["N"])
+    p = _plan(dim=3, n=n, nu=float(g["nu"]), dt=float(g["dt"]))
+    uh = _c64(g["u_hat0"])
+    u = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
+    p.step(uh, int(g["steps"]), u_out=u)
+    assert _rel(uh.cpu().numpy(), g["u_hat"]) < RTOL
+    assert _rel(u.cpu().numpy(), g["u"]) < RTOL
+
+
+def test_step2d_three_components_golden(gold):
+    g = gold("rand2d_n32")
+    p = _plan(dim=2, n=32, nu=float(g["nu"]), dt=float(g["dt"]))
+    uh = _c64(g["u_hat0"])
+    u = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
+    p.step(uh, int(g["steps"]), u_out=u)
+    assert _rel(uh.cpu().numpy(), g["u_hat"]) < RTOL
+    assert _rel(u.cpu().numpy(), g["u"]) < RTOL
+
+
+def test_tgv2d_golden(gold):
+    g = gold("tgv2d_n32")
+    n = int(g["N"])
+    u0, uh0, *_ = R.set_up_solver(n, float(g["nu"]), 2, "TGV2D", float(g["dt"]), 42, 8,
+                                  None, None, "none", warmup=False)
+    p = _plan(dim=2, n=n, nu=float(g["nu"]), dt=float(g["dt"]))
+    uh = _c64(uh0)
+    p.step(uh, 1 + int(g["steps_after_setup"]))  # set_up_solver's warm-up step + 3
+    assert _rel(uh.cpu().numpy(), g["u_hat"]) < RTOL
+
+
+def test_hit_ekin_forcing_golden(gold):
+    g = gold("hit3d_n16_ekin")
+    n, dt = int(g["N"]), float(g["dt"])
+    _, uh0, _, _, _, _, e0, _ = R.set_up_solver(n, float(g["nu"]), 3, "HIT", dt, int(g["seed"]), 8,
+                                                int(g["kf"]), float(g["e_kin_target"]), "ekin_tot",
+                                                warmup=False)
+    assert abs(e0 - float(g["e_kin_init"])) < 1e-12
+    p = _plan(dim=3, n=n, nu=float(g["nu"]), dt=dt, forcing="ekin_tot", kf=int(g["kf"]),
+              e_kin_init=e0)
+    uh = _c64(uh0)
+    steps = 1 + int(g["steps_after_setup"])
+    einj = torch.zeros(steps, dtype=torch.float64, device="cuda")
+    p.step(uh, steps, e_inj=einj)
+    assert _rel(uh.cpu().numpy(), g["u_hat"]) < RTOL
+    np.testing.assert_allclose(einj.cpu().numpy(), g["e_inj"], rtol=1e-3, atol=1e-6)
+    ke = torch.zeros(1, dtype=torch.float64, device="cuda")
+    p.kinetic_energy(uh, ke)
+    assert abs(float(ke) - e0) < 1e-6 * e0  # ekin_tot pins KE to E0
+
+
+def test_tgv64_known_answer():
+    """from_spectralDNS/main_numpy.py:136: KE after 10 steps = 0.124953117517."""
+    n = 64
+    xyz = np.mgrid[:n, :n, :n].astype(float) * 2 * np.pi / n
+    u0 = R.init_u_tgv(*xyz)
+    p = _plan(dim=3, n=n, nu=0.000625, dt=0.01)
+    uh = torch.empty(p.spec_shape, dtype=torch.complex64, device="cuda")
+    p.rfftn(_f32(u0), uh)
+    u = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
+    p.step(uh, 10, u_out=u)
+    ke_phys = 0.5 * float((u.double() ** 2).sum(0).mean())
+    ke = torch.zeros(1, dtype=torch.float64, device="cuda")
+    p.kinetic_energy(uh, ke)
+    assert abs(ke_phys - 0.124953117517) < 2e-7
+    assert abs(float(ke) - 0.124953117517) < 2e-7
+
+
+@pytest.mark.parametrize("n", [128, 256])
+def test_step3d_large_vs_oracle(n):
+    """One RK4 step on a band-limited random field at production sizes."""
+    rng = np.random.default_rng(7)
+    u0 = R.init_u_hit(n, 3, spectrum="k4exp", kp=4.0)
+    u0 *= np.sqrt(0.5 / R.kinetic_energy(u0))
+    R.set_workers(None)
+    try:
+        uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
+        step = R.rk4_wrapper(2e-3, R.rhs_wrapper(n, 5e-3), None, 0.0, "none")
+        _, uh_ref, _ = step(u0, uh0)
+    finally:
+        R.set_workers(1)
+    p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3)
+    uh = _c64(uh0)
+    p.step(uh, 1)
+    assert _rel(uh.cpu().numpy(), uh_ref) < RTOL
+    del rng
