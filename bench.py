@@ -1,0 +1,399 @@
+"""Throughput of the l3es pseudo-spectral DNS step on GB300 (one JSON line).
+
+Workload (the metric's configuration): 3D forced homogeneous isotropic turbulence on
+[0, 2 pi)^3 at 256^3, FP32 bulk with FP64 reductions; Rogallo initial field with
+E(k) ~ k^4 exp(-2 (k/4)^2), seeded phases, KE 0.5; constant-power forcing eps = 0.1
+on 0 < |k| <= 2; nu = 5e-3; dt from CFL 0.5 (fixed); 32^3 particles uniform in the
+box, interpolated from the 32^3 spectral coarsening by type-2 NUFFT (sigma 2,
+width 6) and advected every step. A step = one RK4 step + coarsening + NUFFT +
+advection. Data are synthetic and seeded.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+N > 1 (under torchrun) runs independent replicas, one per GPU (the path does not
+shard); value = all ranks' steps / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "ql-les-data_gb300")]
+
+METRIC = "RK4 steps/s at 256^3 HIT: FP32 form vs FP64 plain, same GB300, <=1e-5 rel KE err"
+N_GRID = 256
+NU = 5e-3
+EPS_INJ = 0.1
+KF = 2
+KP = 4.0
+KE0 = 0.5
+CFL = 0.5
+SEED = 0
+CKP_N = 32
+WITH_PARTICLES = True  # coarsening + NUFFT + advection inside the step
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (median SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def initial_field(n):
+    """Host FP64 initial field of the workload (product init, l3es.init_fields)."""
+    from l3es import init_fields as F
+
+    u = F.init_u_hit(n, SEED, spectrum="k4exp", kp=KP)
+    u *= np.sqrt(KE0 / (0.5 * np.mean(np.sum(u * u, axis=0))))
+    dx = 2 * np.pi / n
+    umax = np.abs(u).max(axis=(1, 2, 3))
+    dt = CFL / (umax / dx + NU / dx**2).min()  # comp_dt (spectral_solver.py:123-127)
+    return u, float(dt)
+
+
+def particles(c, seed=SEED):
+    rng = np.random.default_rng(seed + 1)
+    return rng.uniform(0.0, 2 * np.pi, size=(c**3, 3))
+
+
+# ---------------------------------------------------------------------------------
+# reference arm / CPU baseline: the FP64 NumPy restatement on the host cores
+# ---------------------------------------------------------------------------------
+def cpu_step_rate(n, steps, warmup, u0=None, dt=None):
+    from oracle import numpy_ref as R
+    from oracle import nufft_ref as NU_
+
+    cores = os.cpu_count() or 1
+    R.set_workers(cores)
+    if u0 is None:
+        u0, dt = initial_field(n)
+    uh = R._rfftn(u0, axes=(1, 2, 3))
+    mask = R.init_forcing_mask_hit(n, KF)
+    step = R.rk4_wrapper(dt, R.rhs_wrapper(n, NU, const_power=(EPS_INJ, mask)), None, 0.0, "none")
+    r = particles(CKP_N)
+    u = u0
+
+    def one(u, uh, r):
+        u, uh, _ = step(u, uh)
+        if not WITH_PARTICLES:
+            return u, uh, r
+        u_l = R.spectral_filtering(u, CKP_N)
+        ur = NU_.interpolate_nufft(u_l, r, w=6)
+        return u, uh, R.shift_fn(r, dt * ur)
+
+    for _ in range(warmup):
+        u, uh, r = one(u, uh, r)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        u, uh, r = one(u, uh, r)
+    el = time.perf_counter() - t0
+    R.set_workers(1)
+    return steps / el, cores
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    steps, warmup = max(1, min(args.steps, 2)), min(args.warmup, 1)
+    rate, cores = cpu_step_rate(args.n, steps, warmup)
+    sample = f"{steps} timed + {warmup} warm-up steps of the {args.n}^3 workload, FP64 NumPy/SciPy"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1e3 / rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"hit3d_{args.n}_forced_const_power_particles{CKP_N}^3", "n": args.n},
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------
+# FP64 plain form on the same GPU: the reference algorithm restated with torch.fft
+# (cuFFT) in complex128, op for op (spectral_solver.py:27-120). Comparator only.
+# ---------------------------------------------------------------------------------
+def fp64_plain_rate(u0, dt, n, steps, warmup):
+    import torch
+
+    dev = "cuda"
+    kx = torch.fft.fftfreq(n, 1.0 / n, dtype=torch.float64, device=dev)
+    kz = kx[: n // 2 + 1].clone()
+    kz[-1] *= -1
+    kkk = torch.stack(torch.meshgrid(kx, kx, kz, indexing="ij"))
+    kkk2 = (kkk * kkk).sum(0)
+    kok2 = kkk / torch.where(kkk2 == 0, torch.ones_like(kkk2), kkk2)
+    kmax = 2.0 / 3.0 * (n // 2 + 1)
+    dealias = ((kkk.abs() < kmax).all(0)).to(torch.float64)
+    band = ((kkk2 > 0) & (kkk2 <= KF * KF)).to(torch.float64)
+    wts = torch.full((n // 2 + 1,), 2.0, dtype=torch.float64, device=dev)
+    wts[0] = wts[-1] = 1.0
+    axes = (1, 2, 3)
+
+    def rhs(u_hat):
+        u = torch.fft.irfftn(u_hat, s=(n, n, n), dim=axes)
+        curl = torch.fft.irfftn(1j * torch.linalg.cross(kkk.to(u_hat.dtype), u_hat, dim=0), s=(n, n, n), dim=axes)
+        du = torch.fft.rfftn(torch.linalg.cross(u, curl, dim=0), dim=axes)
+        du = du * dealias
+        du = du - (du * kok2).sum(0) * kkk
+        du = du - NU * kkk2 * u_hat
+        ef = 0.5 * float((wts * ((u_hat * band).abs() ** 2).sum(0)).sum()) / float(n) ** 6
+        return du + (EPS_INJ / (2 * ef + 1e-300)) * u_hat * band
+
+    a = [1 / 6, 1 / 3, 1 / 3, 1 / 6]
+    b = [0.5, 0.5, 1.0]
+
+    def step(u_hat):
+        u0_ = u_hat.clone()
+        acc = u_hat.clone()
+        uh = u_hat
+        for rk in range(4):
+            du = rhs(uh)
+            if rk < 3:
+                uh = u0_ + b[rk] * dt * du
+            acc += a[rk] * dt * du
+        return acc
+
+    uh = torch.fft.rfftn(torch.from_numpy(u0).to(dev), dim=axes)
+    for _ in range(warmup):
+        uh = step(uh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        uh = step(uh)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ke = 0.5 * float((wts * (uh.abs() ** 2).sum(0)).sum()) / float(n) ** 6
+    return 1e3 / ms, ke
+
+
+# ---------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    from l3es import _native
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n = args.n
+    u0, dt = initial_field(n)
+    plan = _native.Plan(dim=3, n=n, nu=NU, dt=dt, forcing="const_power", kf=KF, eps_inj=EPS_INJ)
+    uh = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
+    u_dev = torch.from_numpy(u0.astype(np.float32)).cuda()
+    plan.rfftn(u_dev, uh)
+    del u_dev
+    uh0 = uh.clone()
+    stream = torch.cuda.current_stream()
+    r_host = particles(CKP_N)
+    npart = r_host.shape[0]
+    ip = _native.InterpPlan(dim=3, ckp_n=CKP_N, n_fine=n, width=6, np_max=npart)
+    r_buf = [torch.from_numpy(r_host).cuda(), torch.empty(npart, 3, dtype=torch.float64, device="cuda")]
+    u_r = torch.empty(npart, 3, dtype=torch.float64, device="cuda")
+
+    def step():
+        plan.step(uh, 1)
+        if WITH_PARTICLES:
+            # combined.py:97-130, :199: velocity from the post-step field at the old
+            # positions, then the Euler shift
+            ip.set_spectrum(uh)
+            ip.interp(r_buf[0], u_r, backend="nufft", dt=dt, r_out=r_buf[1])
+            r_buf.reverse()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    with Clocks(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = clk.summary()
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    value = world * 1e3 / ms
+
+    # instrumented pass: per-kernel CUDA events for the roofline numerator/denominator
+    plan.timing(True)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    stats = plan.kernel_stats()
+    plan.timing(False)
+    # launches of the particle layer per step (crop, prep, 3 grid passes, memset-free
+    # binning: count + scan + scatter, gather)
+    part_launches = 8 * args.steps if WITH_PARTICLES else 0
+    launches = sum(v[0] for v in stats.values()) + part_launches
+    top = max(stats.items(), key=lambda kv: kv[1][1])
+    name, (nl, tms, tb) = top
+    peak, peak_kind = _peaks()
+    achieved = tb / (tms * 1e-3) / 1e9
+    kernels = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "share": v[1] / sum(x[1] for x in stats.values()),
+                   "gbs": v[2] / (v[1] * 1e-3) / 1e9 if v[1] > 0 else None} for k, v in stats.items()}
+
+    # end to end through the public API with host buffers: per step the state stays
+    # resident (as in the reference), the step's scalar result (KE) comes back to host
+    if args.skip_baselines:
+        e2e_ms = float("nan")
+    # end to end through the public API with host buffers, as the reference's combined
+    # loop holds them: particle positions on the host go in, velocities, new positions
+    # and the kinetic energy come back every step (the field state stays resident)
+    ke_dev = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ke_host = torch.zeros(1, dtype=torch.float64).pin_memory()
+    r_pin = torch.from_numpy(r_host).pin_memory()
+    ur_pin = torch.empty(npart, 3, dtype=torch.float64).pin_memory()
+    r_dev = torch.empty(npart, 3, dtype=torch.float64, device="cuda")
+    r_new = torch.empty_like(r_dev)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(0 if args.skip_baselines else args.steps):
+        r_dev.copy_(r_pin, non_blocking=True)
+        plan.step(uh, 1)
+        ip.set_spectrum(uh)
+        ip.interp(r_dev, u_r, backend="nufft", dt=dt, r_out=r_new)
+        plan.kinetic_energy(uh, ke_dev)
+        ur_pin.copy_(u_r, non_blocking=True)
+        r_pin.copy_(r_new, non_blocking=True)
+        ke_host.copy_(ke_dev, non_blocking=True)
+        stream.synchronize()
+    if not args.skip_baselines:
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    h2d = npart * 3 * 8
+    d2h = 2 * npart * 3 * 8 + 8
+
+    line = None
+    if rank == 0 and args.skip_baselines:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "ms_per_step": ms,
+                "note": "--skip-baselines (profiling run): no comparator, CPU or e2e legs"}
+    elif rank == 0:
+        # FP64 plain comparator (a few steps) and the CPU baseline sample
+        fp64_rate, _ = fp64_plain_rate(u0, dt, n, steps=max(2, min(args.steps, 5)), warmup=1)
+        cpu_rate, cores = cpu_step_rate(n, 1, 0, u0=u0, dt=dt)
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (fp64 reductions)", "data": "synthetic",
+            "config": {"workload": f"hit3d_{n}_forced_const_power_particles{CKP_N}^3", "n": n, "nu": NU, "dt": dt,
+                       "particles": f"{npart} uniform, NUFFT sigma=2 w=6 from the {CKP_N}^3 coarsening, Euler",
+                       "forcing": f"const_power eps={EPS_INJ} 0<|k|<={KF}", "init": f"rogallo k4exp kp={KP} KE={KE0}",
+                       "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "l2": "working set (~1.3 GB) larger than L2, no flush"},
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "algo_bytes_per_launch": tb / nl, "ms_per_launch": tms / nl},
+            "kernels": kernels,
+            "fp64_plain": {"value": fp64_rate, "unit": "steps/s", "speedup": value / world / fp64_rate},
+            "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": f"1 step at {n}^3 (RK4 + filter + NUFFT + advection), FP64 NumPy/SciPy"},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "workspace_gb": plan.workspace_bytes / 1e9,
+        }
+    del uh0
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--skip-baselines", action="store_true",
+                    help="profiling runs: time our step only (no FP64 plain, CPU or e2e legs)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -72,6 +72,22 @@ int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count);
 /* Scratch bytes the plan holds on the device (for capacity planning). */
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
 
+/* Per-launch CUDA-event timing of the plan's kernels (tracing; the reference
+ * only wall-clocks whole steps, spectral_solver.py:310-313). enable=1 clears the
+ * counters and records an event pair around every launch on the call's stream;
+ * enable=0 stops recording. */
+int l3es_plan_timing(l3es_plan* plan, int32_t enable);
+
+/* Totals for one kernel kind since timing was enabled (waits for the recorded
+ * launches): summed device time, launch count and summed algorithmic bytes
+ * (logical reads + writes, the roofline numerator). */
+int l3es_plan_kernel_stats(l3es_plan* plan, int32_t kind, double* total_ms, int64_t* launches,
+                           double* algo_bytes);
+
+/* Number of kernel kinds and their names (for l3es_plan_kernel_stats). */
+int32_t l3es_kernel_kind_count(void);
+const char* l3es_kernel_kind_name(int32_t kind);
+
 /* nsteps calls of step_fn(u, u_hat) (l3es/spectral_solver.py:73-118), in place on
  * u_hat. u_out (nullable) receives irfftn(u_hat) after the last step (:114-116).
  * e_inj_dev (nullable, device, nsteps*batch doubles) receives the per-step
@@ -95,6 +111,47 @@ int l3es_irfftn(l3es_plan* plan, const void* u_hat, float* u, void* stream);
 /* Kinetic energy 0.5 mean(sum u^2) of irfftn(u_hat), by Parseval in FP64
  * (spectral_solver.py:318, :94). out_dev: device, batch doubles. */
 int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, void* stream);
+
+/* ---- particle layer: spectral coarsening, NUFFT interpolation, advection ---- */
+
+typedef struct l3es_interp_plan l3es_interp_plan;
+
+/* Interpolator of spectral_interpolator_wrapper(ckp_N, fft_axes, splits, backend)
+ * (l3es/integrator.py:26-34) plus the coarse grid of spectral_filtering
+ * (l3es/utils.py:100-138). n_fine: grid of the spectra passed to
+ * l3es_interp_set_spectrum (0 = coarse fields only); ckp_n: 16, 32, 64 or 128;
+ * width: ES kernel width (4, 6 or 8; upsampling 2); np_max: particle capacity. */
+int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width,
+                            int64_t np_max, l3es_interp_plan** out);
+int l3es_interp_plan_destroy(l3es_interp_plan* plan);
+
+/* Coarse spectrum of spectral_filtering(irfftn(u_hat), ckp_N) taken directly from
+ * the fine half spectrum (no fine-grid FFT): modes k in [-c/2, c/2-1]^dim scaled
+ * by (c/N)^dim, Hermitian-averaged like real(ifftn(.)) (utils.py:115-127). */
+int l3es_interp_set_spectrum(l3es_interp_plan* plan, const void* u_hat_fine, void* stream);
+
+/* Coarse spectrum from a coarse physical field (3, c, c, c) / (3, c, c, 1), i.e. the
+ * np.fft.fftn(u) of interpolate_finufft / interpolate_dft (integrator.py:38, :65). */
+int l3es_interp_set_field(l3es_interp_plan* plan, const float* u_coarse, void* stream);
+
+/* The coarse physical field: spectral_filtering's output (utils.py:126-127),
+ * float32 (3, c, c, c) / (3, c, c, 1). */
+int l3es_interp_coarse_field(l3es_interp_plan* plan, float* u_coarse, void* stream);
+
+/* Copy of the current coarse half spectrum (3, c, c, c/2+1) / (3, c, c/2+1). */
+int l3es_interp_coarse_spectrum(l3es_interp_plan* plan, void* out, void* stream);
+
+/* u_r[j] = Re sum_k Hhat(k) exp(i k.r_j) / c^dim at np particles r (float64,
+ * (np, dim)), into u_r (float64, (np, dim)): interpolate_finufft (backend 0, type-2
+ * NUFFT, integrator.py:36-60) or interpolate_dft (backend 1, exact, :62-91).
+ * r_out (nullable): shift_fn(r, dt * u_r) (integrator.py:21-23, combined.py:199). */
+int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r,
+                int32_t backend, double dt, double* r_out, void* stream);
+
+/* shift_fn(r, scale * dr) = (r + scale * dr) mod box, elementwise over n doubles
+ * (l3es/integrator.py:21-23). */
+int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,
+               double* out, void* stream);
 
 /* Last error message of the calling thread ("" if none). */
 const char* l3es_last_error(void);

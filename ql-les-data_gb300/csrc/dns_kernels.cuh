@@ -6,14 +6,15 @@
 // i.e. a half axis of H = N/2+1 complex64 values, preceded by a "middle" axis
 // (3D: N values, 2D: none) and the full x axis.
 //
-// One right-hand side evaluation (l3es/spectral_solver.py:50-60) is five passes:
-//   kx_inv      x-axis inverse c2c of u_hat and of i k x u_hat (curl prologue)
-//   ky_pass     y-axis inverse c2c (3D only), 6 fields in place
-//   line_cross  half-axis c2r of the 6 fields, u x curl in registers, r2c of the
-//               3 products, stored only for the kept (dealiased) half-axis modes
-//   ky_pass     y-axis forward c2c (3D only), stored only for kept ky rows
-//   kx_fwd_epi  x-axis forward c2c + dealias mask, Leray projection, viscosity,
-//               optional extension terms and the RK4 stage combination
+// One right-hand side evaluation + RK stage (l3es/spectral_solver.py:50-60, :74-80)
+// is six passes:
+//   kx_inv       x-axis inverse c2c of u_hat and of i k x u_hat (curl prologue)
+//   ky_pass      y-axis inverse c2c (3D only), 6 fields in place
+//   line_cross   half-axis c2r of the 6 fields, u x curl, r2c of the 3 products,
+//                stored only for the kept (dealiased) half-axis modes
+//   ky_pass      y-axis forward c2c (3D only), stored only for kept ky rows
+//   kx_fwd_band  x-axis forward c2c on the kept band, dealias mask, Leray projection
+//   k_rk_update  elementwise viscosity, extension terms and RK4 stage combination
 // Intermediate fields never exist in physical space in HBM.
 #pragma once
 
@@ -23,13 +24,19 @@ namespace l3es {
 
 constexpr int TW = 8;  // pencils (columns) per CTA in the strided x / y passes
 
+// Half-axis line passes: one line (an M = N/2 point complex FFT) per T = M/8
+// threads, all in one warp, so the FFT exchanges use __syncwarp only and warps run
+// independently. 4 warps per CTA.
 template <int N>
 struct LineCfg {
   static constexpr int M = N / 2;                 // half-length complex FFT
   static constexpr int E = Fft<M>::E;
   static constexpr int T = Fft<M>::T;             // threads per line
-  static constexpr int LPC = T >= 32 ? 4 : 8;     // lines per CTA
-  static constexpr int THREADS = LPC * T;
+  static_assert(T <= 32, "line passes need the line inside one warp (N <= 512)");
+  static constexpr int LPW = 32 / T;              // lines per warp
+  static constexpr int THREADS = 128;
+  static constexpr int LPC = LPW * (THREADS / 32);  // lines per CTA
+  static constexpr int XS = xpad_len<1>(M);       // exchange slots per line
 };
 
 // wavenumber vector (reference kkk, spectral_solver.py:32-39): 3D (kx, kmid, khalf),
@@ -58,7 +65,7 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
   constexpr int NF = CURL ? 6 : 3;
-  __shared__ float2 sm[xpad_len(N) * TW];
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
   const int p = threadIdx.x % TW, t = threadIdx.x / TW;
   const int m = blockIdx.x * TW + p;
   const bool ok = m < MC;
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(TW * Fft<N>::T)
 ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
         const float2* __restrict__ tw) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  __shared__ float2 sm[xpad_len(N) * TW];
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
   const int p = threadIdx.x % TW, t = threadIdx.x / TW;
   const int col = blockIdx.x * TW + p;
   const bool ok = col < ncols;
@@ -132,10 +139,10 @@ ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
 }
 
 // Hermitian half-spectrum X[0..M] -> packed z (z[n] = x[2n] + i x[2n+1]) input of an
-// M-point inverse FFT (numpy irfft semantics: Im X[0] and Im X[M] are ignored).
-__device__ __forceinline__ float2 c2r_pack(const float2* __restrict__ X, int k, int M,
-                                           const float2* __restrict__ twN, float scale) {
-  float2 a = X[k], b = X[M - k];
+// M-point inverse FFT (numpy irfft semantics: Im X[0] and Im X[M] are ignored):
+//   Z[k] = (X[k] + conj X[M-k]) + i exp(+2 pi i k/N) (X[k] - conj X[M-k]).
+__device__ __forceinline__ float2 c2r_pack_pair(float2 a, float2 b, int k, const float2* __restrict__ twN,
+                                                float scale) {
   if (k == 0) {
     a.y = 0.f;
     b.y = 0.f;
@@ -147,12 +154,37 @@ __device__ __forceinline__ float2 c2r_pack(const float2* __restrict__ X, int k, 
   return make_float2(scale * (s.x + id.x), scale * (s.y + id.y));
 }
 
+// Loads one half-spectrum line for an M-point c2r by T = M/E threads of one warp
+// (thread t holds k = t + T e) and packs it. X[k] is read once per element: the
+// partner X[M-k] lives in thread (T - t) mod T, slot E-1-e (slot (E-e) mod E for
+// t = 0, plus X[M] for k = 0), and arrives by warp shuffle.
+template <int M, int E>
+__device__ __forceinline__ void c2r_load_pack(const float2* __restrict__ X, int t, float2 (&v)[E],
+                                              const float2* __restrict__ twN, float scale) {
+  constexpr int T = M / E;
+  float2 xk[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) xk[e] = __ldg(X + t + T * e);
+  const float2 xm = __ldg(X + M);  // Nyquist, used by t = 0
+  const int lane = threadIdx.x & 31;
+  const int src = lane - t + (t == 0 ? 0 : T - t);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const float2 give = (t == 0) ? xk[(E - e) % E] : xk[E - 1 - e];
+    float2 b;
+    b.x = __shfl_sync(0xffffffffu, give.x, src);
+    b.y = __shfl_sync(0xffffffffu, give.y, src);
+    if (t == 0 && e == 0) b = xm;
+    v[e] = c2r_pack_pair(xk[e], b, t + T * e, twN, scale);
+  }
+}
+
 // M-point forward FFT output Z (exchange buffer, padded index) -> r2c value X[k],
 // k in [0, M] (Z is M-periodic; W^M = -1 gives X[M] = Re Z0 - Im Z0).
 __device__ __forceinline__ float2 r2c_unpack(const float2* Z, int k, int M,
                                              const float2* __restrict__ twN) {
-  const float2 zk = Z[xpad(k < M ? k : 0)];
-  const float2 zm = Z[xpad(k == 0 ? 0 : M - k)];
+  const float2 zk = Z[xpad<1>(k < M ? k : 0)];
+  const float2 zm = Z[xpad<1>(k == 0 ? 0 : M - k)];
   const float2 s = make_float2(zk.x + zm.x, zk.y - zm.y);
   const float2 d = make_float2(zk.x - zm.x, zk.y + zm.y);
   const float2 id = mul_i<kFwd>(cmul(__ldg(twN + k), d));  // -i W^k d
@@ -161,77 +193,79 @@ __device__ __forceinline__ float2 r2c_unpack(const float2* Z, int k, int M,
 
 // ------------------------------------------------------------------------------
 // Half-axis line pass of the RHS: 6 half-spectrum lines (u, curl u) -> c2r -> u x
-// curl u in registers -> r2c of the 3 products, written for k <= kd (zeros up to kt).
-// scale normalises each inverse transform (1/N^dim). Lines are contiguous rows of H.
+// curl u -> r2c of the 3 products, written for k <= kd (zeros up to kt). scale
+// normalises each inverse transform (1/N^dim). Lines are contiguous rows of H.
+// Physical u is parked in shared memory (same thread writes and reads it), the
+// cross product accumulates in registers while the curl lines are transformed.
 // ------------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(LineCfg<N>::THREADS)
+__global__ void __launch_bounds__(LineCfg<N>::THREADS, 3)
 line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, long long ds,
-           int kt, int kd, float scale, const float2* __restrict__ twN, int lines_per_batch) {
+           int kt, int kd, float scale, const float2* __restrict__ twN, int nlines) {
   using C = LineCfg<N>;
   constexpr int M = C::M, H = N / 2 + 1, E = C::E, T = C::T, LPC = C::LPC;
-  extern __shared__ float2 dsm[];
-  float2* s_in = dsm;                   // [6][LPC * H]
-  float2* s_x = dsm + 6 * LPC * H;      // [LPC][xpad_len(M)]
+  __shared__ float2 s_x[LPC * C::XS];
+  __shared__ float2 s_u[LPC * 3 * M];
   const int batch = blockIdx.y;
-  const long long line0 = (long long)blockIdx.x * LPC;
-  const float2* wb = w + (long long)batch * 6 * fs;
-  float2* db = du + (long long)batch * 3 * ds;
-#pragma unroll 1
-  for (int f = 0; f < 6; ++f) {
-    const float2* src = wb + f * fs + line0 * H;
-    for (int i = threadIdx.x; i < LPC * H; i += blockDim.x) s_in[f * LPC * H + i] = src[i];
-  }
-  __syncthreads();
   const int q = threadIdx.x / T, t = threadIdx.x % T;
-  float2* xs = s_x + q * xpad_len(M);
-  float2 u[3][E], cr[3][E];
+  const long long line_raw = (long long)blockIdx.x * LPC + q;
+  const bool valid = line_raw < nlines;
+  const long long line = valid ? line_raw : nlines - 1;  // idle lines mirror a valid one
+  const float2* src = w + (long long)batch * 6 * fs + line * H;
+  float2* xs = s_x + q * C::XS;
+  float2* su = s_u + q * 3 * M;
+  float2 cr[3][E];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int e = 0; e < E; ++e) cr[c][e] = make_float2(0.f, 0.f);
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
-    const float2* X = s_in + f * LPC * H + q * H;
     float2 v[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = c2r_pack(X, t + T * e, M, twN, scale);
-    block_fft<M, E, kInv, 1>(v, xs, t, twN, 2);
+    c2r_load_pack<M, E>(src + f * fs, t, v, twN, scale);
+    block_fft<M, E, kInv, 1, true>(v, xs, t, twN, 2);
     // v[e] packs the physical values at 2n and 2n+1, n = t + T*e
 #pragma unroll
     for (int e = 0; e < E; ++e) {
+      const int n = t + T * e;
       const float2 o = v[e];
       if (f < 3) {
-        u[f][e] = o;
+        su[f * M + n] = o;
       } else if (f == 3) {  // curl_x: c_y += u_z w_x, c_z -= u_y w_x
-        cr[1][e].x = fmaf(u[2][e].x, o.x, cr[1][e].x);
-        cr[1][e].y = fmaf(u[2][e].y, o.y, cr[1][e].y);
-        cr[2][e].x = fmaf(-u[1][e].x, o.x, cr[2][e].x);
-        cr[2][e].y = fmaf(-u[1][e].y, o.y, cr[2][e].y);
+        const float2 uz = su[2 * M + n], uy = su[M + n];
+        cr[1][e].x = fmaf(uz.x, o.x, cr[1][e].x);
+        cr[1][e].y = fmaf(uz.y, o.y, cr[1][e].y);
+        cr[2][e].x = fmaf(-uy.x, o.x, cr[2][e].x);
+        cr[2][e].y = fmaf(-uy.y, o.y, cr[2][e].y);
       } else if (f == 4) {  // curl_y: c_x -= u_z w_y, c_z += u_x w_y
-        cr[0][e].x = fmaf(-u[2][e].x, o.x, cr[0][e].x);
-        cr[0][e].y = fmaf(-u[2][e].y, o.y, cr[0][e].y);
-        cr[2][e].x = fmaf(u[0][e].x, o.x, cr[2][e].x);
-        cr[2][e].y = fmaf(u[0][e].y, o.y, cr[2][e].y);
+        const float2 uz = su[2 * M + n], ux = su[n];
+        cr[0][e].x = fmaf(-uz.x, o.x, cr[0][e].x);
+        cr[0][e].y = fmaf(-uz.y, o.y, cr[0][e].y);
+        cr[2][e].x = fmaf(ux.x, o.x, cr[2][e].x);
+        cr[2][e].y = fmaf(ux.y, o.y, cr[2][e].y);
       } else {  // curl_z: c_x += u_y w_z, c_y -= u_x w_z
-        cr[0][e].x = fmaf(u[1][e].x, o.x, cr[0][e].x);
-        cr[0][e].y = fmaf(u[1][e].y, o.y, cr[0][e].y);
-        cr[1][e].x = fmaf(-u[0][e].x, o.x, cr[1][e].x);
-        cr[1][e].y = fmaf(-u[0][e].y, o.y, cr[1][e].y);
+        const float2 uy = su[M + n], ux = su[n];
+        cr[0][e].x = fmaf(uy.x, o.x, cr[0][e].x);
+        cr[0][e].y = fmaf(uy.y, o.y, cr[0][e].y);
+        cr[1][e].x = fmaf(-ux.x, o.x, cr[1][e].x);
+        cr[1][e].y = fmaf(-ux.y, o.y, cr[1][e].y);
       }
     }
-    __syncthreads();
+    __syncwarp();
   }
+  float2* db = du + (long long)batch * 3 * ds + line * kt;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    block_fft<M, E, kFwd, 1>(cr[c], xs, t, twN, 2);
-    __syncthreads();
+    block_fft<M, E, kFwd, 1, true>(cr[c], xs, t, twN, 2);
+    __syncwarp();
 #pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad(t + T * e)] = cr[c][e];
-    __syncthreads();
-    float2* dst = db + c * ds + (line0 + q) * kt;
-    for (int k = t; k < kt; k += T) dst[k] = k <= kd ? r2c_unpack(xs, k, M, twN) : make_float2(0.f, 0.f);
-    __syncthreads();
+    for (int e = 0; e < E; ++e) xs[xpad<1>(t + T * e)] = cr[c][e];
+    __syncwarp();
+    if (valid) {
+      float2* dst = db + c * ds;
+      for (int k = t; k < kt; k += T) dst[k] = k <= kd ? r2c_unpack(xs, k, M, twN) : make_float2(0.f, 0.f);
+    }
+    __syncwarp();
   }
 }
 
@@ -241,29 +275,28 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
 template <int N>
 __global__ void __launch_bounds__(LineCfg<N>::THREADS)
 line_c2r(const float2* __restrict__ w, long long fs, float* __restrict__ out, long long os,
-         float scale, const float2* __restrict__ twN) {
+         float scale, const float2* __restrict__ twN, int nlines) {
   using C = LineCfg<N>;
   constexpr int M = C::M, H = N / 2 + 1, E = C::E, T = C::T, LPC = C::LPC;
-  extern __shared__ float2 dsm[];
-  float2* s_in = dsm;               // [LPC * H]
-  float2* s_x = dsm + LPC * H;      // [LPC][xpad_len(M)]
+  __shared__ float2 s_x[LPC * C::XS];
   const int batch = blockIdx.y;
-  const long long line0 = (long long)blockIdx.x * LPC;
   const int q = threadIdx.x / T, t = threadIdx.x % T;
-  float2* xs = s_x + q * xpad_len(M);
+  const long long line_raw = (long long)blockIdx.x * LPC + q;
+  const bool valid = line_raw < nlines;
+  const long long line = valid ? line_raw : nlines - 1;
+  float2* xs = s_x + q * C::XS;
 #pragma unroll 1
   for (int f = 0; f < 3; ++f) {
-    const float2* src = w + (long long)batch * 3 * fs + f * fs + line0 * H;
-    for (int i = threadIdx.x; i < LPC * H; i += blockDim.x) s_in[i] = src[i];
-    __syncthreads();
+    const float2* src = w + (long long)batch * 3 * fs + f * fs + line * H;
     float2 v[E];
+    c2r_load_pack<M, E>(src, t, v, twN, scale);
+    block_fft<M, E, kInv, 1, true>(v, xs, t, twN, 2);
+    if (valid) {
+      float2* dst = reinterpret_cast<float2*>(out + (long long)batch * 3 * os + f * os + line * N);
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = c2r_pack(s_in + q * H, t + T * e, M, twN, scale);
-    block_fft<M, E, kInv, 1>(v, xs, t, twN, 2);
-    float2* dst = reinterpret_cast<float2*>(out + (long long)batch * 3 * os + f * os + (line0 + q) * N);
-#pragma unroll
-    for (int e = 0; e < E; ++e) dst[t + T * e] = v[e];
-    __syncthreads();
+      for (int e = 0; e < E; ++e) dst[t + T * e] = v[e];
+    }
+    __syncwarp();
   }
 }
 
@@ -273,30 +306,32 @@ line_c2r(const float2* __restrict__ w, long long fs, float* __restrict__ out, lo
 template <int N>
 __global__ void __launch_bounds__(LineCfg<N>::THREADS)
 line_r2c(const float* __restrict__ in, long long is, float2* __restrict__ w, long long fs,
-         const float2* __restrict__ twN) {
+         const float2* __restrict__ twN, int nlines) {
   using C = LineCfg<N>;
   constexpr int M = C::M, H = N / 2 + 1, E = C::E, T = C::T, LPC = C::LPC;
-  extern __shared__ float2 dsm[];
-  float2* s_x = dsm;  // [LPC][xpad_len(M)]
+  __shared__ float2 s_x[LPC * C::XS];
   const int batch = blockIdx.y;
-  const long long line0 = (long long)blockIdx.x * LPC;
   const int q = threadIdx.x / T, t = threadIdx.x % T;
-  float2* xs = s_x + q * xpad_len(M);
+  const long long line_raw = (long long)blockIdx.x * LPC + q;
+  const bool valid = line_raw < nlines;
+  const long long line = valid ? line_raw : nlines - 1;
+  float2* xs = s_x + q * C::XS;
 #pragma unroll 1
   for (int f = 0; f < 3; ++f) {
-    const float2* src =
-        reinterpret_cast<const float2*>(in + (long long)batch * 3 * is + f * is + (line0 + q) * N);
+    const float2* src = reinterpret_cast<const float2*>(in + (long long)batch * 3 * is + f * is + line * N);
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = src[t + T * e];
-    block_fft<M, E, kFwd, 1>(v, xs, t, twN, 2);
-    __syncthreads();
+    for (int e = 0; e < E; ++e) v[e] = __ldg(src + t + T * e);
+    block_fft<M, E, kFwd, 1, true>(v, xs, t, twN, 2);
+    __syncwarp();
 #pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad(t + T * e)] = v[e];
-    __syncthreads();
-    float2* dst = w + (long long)batch * 3 * fs + f * fs + (line0 + q) * H;
-    for (int k = t; k < H; k += T) dst[k] = r2c_unpack(xs, k, M, twN);
-    __syncthreads();
+    for (int e = 0; e < E; ++e) xs[xpad<1>(t + T * e)] = v[e];
+    __syncwarp();
+    if (valid) {
+      float2* dst = w + (long long)batch * 3 * fs + f * fs + line * H;
+      for (int k = t; k < H; k += T) dst[k] = r2c_unpack(xs, k, M, twN);
+    }
+    __syncwarp();
   }
 }
 
@@ -310,7 +345,7 @@ kx_fwd_plain(const float2* __restrict__ w, long long fs, float2* __restrict__ uh
   constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
-  __shared__ float2 sm[xpad_len(N) * TW];
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
   const int p = threadIdx.x % TW, t = threadIdx.x / TW;
   const int m = blockIdx.x * TW + p;
   const bool ok = m < MC;
@@ -330,7 +365,7 @@ kx_fwd_plain(const float2* __restrict__ w, long long fs, float2* __restrict__ uh
   }
 }
 
-// RK4 stage combination and extension terms for the epilogue.
+// RK4 stage combination and extension terms for the elementwise update.
 struct EpiParams {
   float a_dt;        // a_rk4[rk] * dt
   float b_dt;        // b_rk4[rk] * dt (rk < 3)
@@ -360,113 +395,157 @@ __device__ __forceinline__ void block_sum_store(double v, double* partial, int b
 }
 
 // ------------------------------------------------------------------------------
-// x-axis forward pass of the nonlinear term + RHS/RK4 epilogue
-// (spectral_solver.py:56-59 and :74-80). CTA = (half-axis tile, middle index).
-// Tiles inside the dealiased band run the FFT; the others only apply the linear
-// terms (their nonlinear contribution is masked to zero).
-//   rk 0   : us = u0 = S (read),   acc <- u0 + a dt du,  out <- u0 + b dt du
-//   rk 1,2 : us = out (read),      acc += a dt du,       out <- u0 + b dt du
-//   rk 3   : us = out (read),      fin <- acc + a dt du
-//   rk -1  : out <- du (the reference's rhs_fn)
+// x-axis forward pass of the nonlinear term on the dealiased band only
+// (spectral_solver.py:55-58: du *= dealias; du -= (sum du.k/k^2) k). CTA = (half-axis
+// tile inside kt, middle-axis row inside the band). Output P keeps only the kept
+// modes: P[c][kx + kd][kmid + kd][kh] (3D), P[c][kx + kd][kh] (2D), kh < kt, with
+// zeros for kh > kd.
 // ------------------------------------------------------------------------------
 template <int N, int DIM>
 __global__ void __launch_bounds__(TW * Fft<N>::T)
-kx_fwd_epi(const float2* __restrict__ du, long long dcs, int kt, int kd,
-           // us/out alias (stage buffer updated in place), so no __restrict__ here
-           const float2* us, const float2* u0, float2* acc, float2* out, float2* fin,
-           long long cs, EpiParams prm,
-           const double* __restrict__ band_scale, double* __restrict__ partial,
-           const float2* __restrict__ tw) {
-  constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
+kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
+            const float2* __restrict__ tw) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
   constexpr int NMID = DIM == 3 ? N : 1;
-  __shared__ float2 sm[xpad_len(N) * TW];
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
   const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int mid = blockIdx.y;
-  const int km = DIM == 3 ? kfull(mid, N) : 0;
-  const int kh = blockIdx.x * TW + p;
-  const bool okh = kh < H;
+  const int nb = 2 * kd + 1;
+  const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
+  const int km = DIM == 3 ? kmb - kd : 0;
+  const int mid = km < 0 ? km + N : km;
+  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
   const int batch = blockIdx.z;
-  const long long bd = (long long)batch * 3 * dcs, bu = (long long)batch * 3 * cs;
-  const bool fft_path = (km <= kd && -km <= kd) && (blockIdx.x * TW < kt);
+  const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
   float2 d[3][E];
-  if (fft_path) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
+  for (int c = 0; c < 3; ++c)
 #pragma unroll
-      for (int e = 0; e < E; ++e)
-        d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
+    for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      block_fft<N, E, kFwd, TW>(d[c], sm + p, t, tw, 1);
-      __syncthreads();
-    }
+  for (int c = 0; c < 3; ++c) {
+    block_fft<N, E, kFwd, TW>(d[c], sm + p, t, tw, 1);
+    __syncthreads();
   }
-  float fscale = 0.f;
-  if (prm.band_kf2 > 0) fscale = (float)band_scale[batch];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int kx = kfull(t + T * e, N);
+    if (kx > kd || -kx > kd) continue;
+    float k0, k1, k2;
+    kvec<DIM>(kx, km, kh, k0, k1, k2);
+    const bool keep = kh <= kd;
+    const int ik2 = kx * kx + km * km + kh * kh;
+    const float inv = 1.0f / (ik2 == 0 ? 1.0f : (float)ik2);
+    const float2 v0 = keep ? d[0][e] : make_float2(0.f, 0.f);
+    const float2 v1 = keep ? d[1][e] : make_float2(0.f, 0.f);
+    const float2 v2 = keep ? d[2][e] : make_float2(0.f, 0.f);
+    const float pr = (v0.x * k0 + v1.x * k1 + v2.x * k2) * inv;
+    const float pi_ = (v0.y * k0 + v1.y * k1 + v2.y * k2) * inv;
+    const long long o = bp + ((long long)(kx + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
+    P[o] = make_float2(v0.x - pr * k0, v0.y - pi_ * k0);
+    P[o + pcs] = make_float2(v1.x - pr * k1, v1.y - pi_ * k1);
+    P[o + 2 * pcs] = make_float2(v2.x - pr * k2, v2.y - pi_ * k2);
+  }
+}
+
+// ------------------------------------------------------------------------------
+// Elementwise linear terms + RK4 stage combination (spectral_solver.py:59, :74-80),
+// two complex values (one float4) per thread over all 3 components:
+//   du = P(k) (kept band, else 0) - nu k^2 us [- drag us + forcing terms]
+//   rk 0   : acc <- us + a dt du,  out <- us + b dt du         (us = u0)
+//   rk 1,2 : acc += a dt du,       out <- u0 + b dt du         (us aliases out)
+//   rk 3   : fin <- acc + a dt du
+//   rk -1  : out <- du (the reference's rhs_fn)
+// Every thread loads all its operands before storing (us/out and acc alias).
+// ------------------------------------------------------------------------------
+template <int N, int DIM>
+__device__ __forceinline__ float2 rk_elem(long long i, int c, float2 sv, float2 a0, float2 z0,
+                                          const float2* __restrict__ P, long long pcs, int kt, int kd,
+                                          const EpiParams& prm, float fscale, float2& nv, double& esum) {
+  constexpr int H = N / 2 + 1;
+  constexpr int NMID = DIM == 3 ? N : 1;
+  const int kh = (int)(i % H);
+  const long long rest = i / H;
+  const int mid = (int)(rest % NMID);
+  const int kxi = (int)(rest / NMID);
+  const int kx = kfull(kxi, N);
+  const int km = DIM == 3 ? kfull(mid, N) : 0;
+  const int ik2 = kx * kx + km * km + kh * kh;
+  const float kk2 = (float)ik2;
+  float2 r = make_float2(0.f, 0.f);
+  // band rows as unsigned offsets: in the band iff 0 <= k + kd <= 2 kd on every axis
+  const unsigned nb = 2u * (unsigned)kd + 1u;
+  const unsigned bx = (unsigned)(kx + kd);
+  const unsigned bm = DIM == 3 ? (unsigned)(km + kd) : 0u;
+  if (bx < nb && bm < nb && (unsigned)kh <= (unsigned)kd) {
+    const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
+    r = __ldg(P + c * pcs + row * kt + kh);
+  }
+  r.x -= prm.nu * kk2 * sv.x;
+  r.y -= prm.nu * kk2 * sv.y;
+  if (prm.drag != 0.f) {
+    r.x -= prm.drag * sv.x;
+    r.y -= prm.drag * sv.y;
+  }
+  if (c == 0 && prm.kolm_k > 0 && kxi == 0 && mid == 0 && kh == prm.kolm_k) r.y += -0.5f * prm.kolm_amp * (float)N * (float)N;
+  if (prm.band_kf2 > 0 && ik2 > 0 && ik2 <= prm.band_kf2) {
+    r.x += fscale * sv.x;
+    r.y += fscale * sv.y;
+  }
+  if (prm.rk < 0) {
+    nv = r;
+    return r;
+  }
+  if (prm.rk == 0) {
+    nv = make_float2(fmaf(prm.b_dt, r.x, sv.x), fmaf(prm.b_dt, r.y, sv.y));
+    return make_float2(fmaf(prm.a_dt, r.x, sv.x), fmaf(prm.a_dt, r.y, sv.y));
+  }
+  if (prm.rk < 3) {
+    nv = make_float2(fmaf(prm.b_dt, r.x, z0.x), fmaf(prm.b_dt, r.y, z0.y));
+    return make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
+  }
+  nv = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
+  if (prm.want_energy) {
+    const double wgt = (kh == 0 || kh == N / 2) ? 1.0 : 2.0;
+    esum += wgt * ((double)nv.x * nv.x + (double)nv.y * nv.y);
+  }
+  return nv;
+}
+
+template <int N, int DIM>
+__global__ void __launch_bounds__(256)
+k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const float2* us, const float2* u0,
+            float2* acc, float2* out, float2* fin, long long cs, EpiParams prm,
+            const double* __restrict__ band_scale, double* __restrict__ partial) {
+  const int batch = blockIdx.y;
+  const long long pairs = 3 * cs / 2;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long bo = (long long)batch * 3 * cs;
+  const float fscale = prm.band_kf2 > 0 ? (float)band_scale[batch] : 0.f;
   double esum = 0.0;
-  if (okh) {
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int kxi = t + T * e;
-      const int kx = kfull(kxi, N);
-      float k0, k1, k2;
-      kvec<DIM>(kx, km, kh, k0, k1, k2);
-      const bool keep = fft_path && (kx <= kd && -kx <= kd) && kh <= kd;
-      const long long idx = ((long long)kxi * NMID + mid) * H + kh;
-      const int ik2 = kx * kx + (DIM == 3 ? km * km : 0) + kh * kh;
-      const float kk2 = (float)ik2;
-      float2 v[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) v[c] = keep ? d[c][e] : make_float2(0.f, 0.f);
-      // Leray projection: du -= (sum_c du_c k_c / k^2) k
-      const float inv = 1.0f / (ik2 == 0 ? 1.0f : kk2);
-      const float pr = (v[0].x * k0 + v[1].x * k1 + v[2].x * k2) * inv;
-      const float pi_ = (v[0].y * k0 + v[1].y * k1 + v[2].y * k2) * inv;
-      const float kc[3] = {k0, k1, k2};
-      const bool band = prm.band_kf2 > 0 && ik2 > 0 && ik2 <= prm.band_kf2;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float2 s = us[bu + c * cs + idx];
-        float2 r;
-        r.x = v[c].x - pr * kc[c] - prm.nu * kk2 * s.x;
-        r.y = v[c].y - pi_ * kc[c] - prm.nu * kk2 * s.y;
-        if (prm.drag != 0.f) {
-          r.x -= prm.drag * s.x;
-          r.y -= prm.drag * s.y;
-        }
-        if (c == 0 && prm.kolm_k > 0 && kxi == 0 && kh == prm.kolm_k) {
-          r.y += -0.5f * prm.kolm_amp * (float)N * (float)N;
-        }
-        if (band) {
-          r.x += fscale * s.x;
-          r.y += fscale * s.y;
-        }
-        const long long o = bu + c * cs + idx;
-        if (prm.rk < 0) {  // right-hand side only (rhs_fn): out <- du
-          out[o] = r;
-        } else if (prm.rk == 0) {
-          acc[o] = make_float2(fmaf(prm.a_dt, r.x, s.x), fmaf(prm.a_dt, r.y, s.y));
-          out[o] = make_float2(fmaf(prm.b_dt, r.x, s.x), fmaf(prm.b_dt, r.y, s.y));
-        } else if (prm.rk < 3) {
-          const float2 a0 = acc[o], z0 = u0[o];
-          acc[o] = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
-          out[o] = make_float2(fmaf(prm.b_dt, r.x, z0.x), fmaf(prm.b_dt, r.y, z0.y));
-        } else {
-          const float2 a0 = acc[o];
-          const float2 nv = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
-          fin[o] = nv;
-          if (prm.want_energy) {
-            const double wgt = (kh == 0 || kh == N / 2) ? 1.0 : 2.0;
-            esum += wgt * ((double)nv.x * nv.x + (double)nv.y * nv.y);
-          }
-        }
-      }
+  if (q < pairs) {
+    const long long g = 2 * q;  // global element (component-major)
+    const float4 s4 = reinterpret_cast<const float4*>(us + bo)[q];
+    float4 a4 = make_float4(0.f, 0.f, 0.f, 0.f), z4 = a4;
+    if (prm.rk > 0) a4 = reinterpret_cast<const float4*>(acc + bo)[q];
+    if (prm.rk > 0 && prm.rk < 3) z4 = reinterpret_cast<const float4*>(u0 + bo)[q];
+    const float2* Pb = P + (long long)batch * 3 * pcs;
+    float2 nv0, nv1;
+    const int c0 = (int)(g / cs), c1 = (int)((g + 1) / cs);
+    const float2 r0 = rk_elem<N, DIM>(g - (long long)c0 * cs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
+                                      make_float2(z4.x, z4.y), Pb, pcs, kt, kd, prm, fscale, nv0, esum);
+    const float2 r1 = rk_elem<N, DIM>(g + 1 - (long long)c1 * cs, c1, make_float2(s4.z, s4.w),
+                                      make_float2(a4.z, a4.w), make_float2(z4.z, z4.w), Pb, pcs, kt, kd, prm,
+                                      fscale, nv1, esum);
+    if (prm.rk < 0) {
+      reinterpret_cast<float4*>(out + bo)[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
+    } else if (prm.rk < 3) {
+      reinterpret_cast<float4*>(acc + bo)[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
+      reinterpret_cast<float4*>(out + bo)[q] = make_float4(nv0.x, nv0.y, nv1.x, nv1.y);
+    } else {
+      reinterpret_cast<float4*>(fin + bo)[q] = make_float4(nv0.x, nv0.y, nv1.x, nv1.y);
     }
   }
-  if (prm.rk == 3 && prm.want_energy) {
-    const int blk = (batch * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    block_sum_store(esum, partial, blk);
-  }
+  if (prm.rk == 3 && prm.want_energy) block_sum_store(esum, partial, batch * gridDim.x + blockIdx.x);
 }
 
 // ------------------------------------------------------------------------------

@@ -13,15 +13,9 @@ struct DnsOps {
   static constexpr int TX = TW * Fft<N>::T;  // threads of the strided passes
   using L = LineCfg<N>;
 
-  static size_t cross_smem() { return (size_t)(6 * L::LPC * H + L::LPC * xpad_len(L::M)) * sizeof(float2); }
-  static size_t c2r_smem() { return (size_t)(L::LPC * H + L::LPC * xpad_len(L::M)) * sizeof(float2); }
-  static size_t r2c_smem() { return (size_t)(L::LPC * xpad_len(L::M)) * sizeof(float2); }
+  static unsigned line_blocks(long long lines) { return (unsigned)((lines + L::LPC - 1) / L::LPC); }
 
-  static void init_attrs() {
-    cudaFuncSetAttribute(line_cross<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cross_smem());
-    cudaFuncSetAttribute(line_c2r<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c2r_smem());
-    cudaFuncSetAttribute(line_r2c<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r2c_smem());
-  }
+  static void init_attrs() {}
 
   // us: field the RHS is evaluated on; S: state; out: RK stage field (or du for rk=-1)
   template <int DIM>
@@ -30,19 +24,39 @@ struct DnsOps {
     const long long mc = c.nmid * H;
     const long long lines = c.nmid * N;
     const float scale = (float)(1.0 / (DIM == 3 ? (double)N * N * N : (double)N * N));
-    kx_inv<N, DIM, true><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(us, c.cs, c.W, c.fs, c.tw);
+    const double B = c.batch, A = 8.0 * 3.0 * c.cs * B;  // bytes of one 3-component spectrum
+    const double Adu = 8.0 * 3.0 * c.ds * B;               // bytes of the truncated DU field
+    const double rows = DIM == 3 ? (2.0 * c.kd + 1.0) / N : 1.0;  // kept y rows
+    L3ES_LAUNCH(c, KK_X_INV, 3.0 * A, s,
+                kx_inv<N, DIM, true><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                    us, c.cs, c.W, c.fs, c.tw));
     if (DIM == 3)
-      ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 6 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2, c.tw);
-    line_cross<N><<<dim3((unsigned)(lines / L::LPC), c.batch), L::THREADS, cross_smem(), s>>>(
-        c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines);
+      L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
+                  ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 6 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                                                                                         c.tw));
+    L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
+                    c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));
     if (DIM == 3)
-      ky_pass<N, kFwd><<<dim3(c.kt / TW, N, 3 * c.batch), TX, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd, c.tw);
+      L3ES_LAUNCH(c, KK_Y_FWD, Adu * (1.0 + rows), s,
+                  ky_pass<N, kFwd><<<dim3(c.kt / TW, N, 3 * c.batch), TX, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd,
+                                                                                  c.tw));
     if (prm.band_kf2 > 0) {
       const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
-      k_band_scale<DIM><<<c.batch, 256, 0, s>>>(us, c.cs, N, c.kf, inv_n2d, c.eps_inj, 1e-30, c.band);
+      L3ES_LAUNCH(c, KK_BAND, 0.0, s,
+                  k_band_scale<DIM><<<c.batch, 256, 0, s>>>(us, c.cs, N, c.kf, inv_n2d, c.eps_inj, 1e-30, c.band));
     }
-    kx_fwd_epi<N, DIM><<<dim3((H + TW - 1) / TW, (unsigned)c.nmid, c.batch), TX, 0, s>>>(
-        c.DU, c.ds, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm, c.band, c.partial, c.tw);
+    // band x-FFT + projection into P, then the elementwise RK update
+    const int nb = 2 * c.kd + 1;
+    const double Ap = 8.0 * 3.0 * c.pcs * B;
+    L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
+                kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
+                    c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw));
+    const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 3.0 : rk < 3 ? 5.0 : 3.0);
+    const long long pairs = 3 * c.cs / 2;
+    L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
+                k_rk_update<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(
+                    c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm, c.band, c.partial));
   }
 
   static void stage(const Ctx& c, const float2* us, float2* S, float2* out, int rk, const EpiParams& prm,
@@ -58,11 +72,17 @@ struct DnsOps {
     const long long mc = c.nmid * H;
     const long long lines = c.nmid * N;
     const float scale = (float)(1.0 / (DIM == 3 ? (double)N * N * N : (double)N * N));
-    kx_inv<N, DIM, false><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(uh, c.cs, c.W, c.fs, c.tw);
+    const double A = 8.0 * 3.0 * c.cs * c.batch, P = 4.0 * 3.0 * c.ps * c.batch;
+    L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
+                kx_inv<N, DIM, false><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                    uh, c.cs, c.W, c.fs, c.tw));
     if (DIM == 3)
-      ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2, c.tw);
-    line_c2r<N><<<dim3((unsigned)(lines / L::LPC), c.batch), L::THREADS, c2r_smem(), s>>>(c.W, c.fs, u, c.ps,
-                                                                                          scale, c.tw);
+      L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
+                  ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                                                                                         c.tw));
+    L3ES_LAUNCH(c, KK_LINE_C2R, A + P, s,
+                line_c2r<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
+                    c.W, c.fs, u, c.ps, scale, c.tw, (int)lines));
   }
 
   static void irfftn(const Ctx& c, const float2* uh, float* u, cudaStream_t s) {
@@ -76,10 +96,17 @@ struct DnsOps {
   static void rfftn_dim(const Ctx& c, const float* u, float2* uh, cudaStream_t s) {
     const long long mc = c.nmid * H;
     const long long lines = c.nmid * N;
-    line_r2c<N><<<dim3((unsigned)(lines / L::LPC), c.batch), L::THREADS, r2c_smem(), s>>>(u, c.ps, c.W, c.fs, c.tw);
+    const double A = 8.0 * 3.0 * c.cs * c.batch, P = 4.0 * 3.0 * c.ps * c.batch;
+    L3ES_LAUNCH(c, KK_LINE_R2C, A + P, s,
+                line_r2c<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
+                    u, c.ps, c.W, c.fs, c.tw, (int)lines));
     if (DIM == 3)
-      ky_pass<N, kFwd><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2, c.tw);
-    kx_fwd_plain<N, DIM><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(c.W, c.fs, uh, c.cs, c.tw);
+      L3ES_LAUNCH(c, KK_Y_FWD, 2.0 * A, s,
+                  ky_pass<N, kFwd><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                                                                                         c.tw));
+    L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 2.0 * A, s,
+                kx_fwd_plain<N, DIM><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                    c.W, c.fs, uh, c.cs, c.tw));
   }
 
   static void rfftn(const Ctx& c, const float* u, float2* uh, cudaStream_t s) {

@@ -134,15 +134,28 @@ struct Sched {
   static constexpr int ns(int s) { return ipow(E, s); }  // Ns before stage s
 };
 
-// Padded exchange index: one spare slot every 8 elements keeps the radix-8 strided
-// writes of the first stage on distinct shared-memory banks. A buffer for n
-// elements holds xpad_len(n) slots.
-__device__ __forceinline__ int xpad(int n) { return n + (n >> 3); }
-__host__ __device__ constexpr int xpad_len(int n) { return n + n / 8; }
+// Exchange index per layout, chosen with a shared-memory bank model (8-byte
+// accesses served per half warp) of every Stockham read/write pattern:
+//  - column-interleaved buffers (SS > 1): one spare slot every 8 elements;
+//  - contiguous per-line buffers (SS == 1): XOR swizzle of the low 4 bits by bits
+//    3..6 (a permutation inside aligned blocks of 16), lines M + 8 slots apart.
+template <int SS>
+__device__ __forceinline__ int xpad(int n) { return SS == 1 ? n ^ ((n >> 3) & 15) : n + (n >> 3); }
+template <int SS>
+__host__ __device__ constexpr int xpad_len(int n) { return SS == 1 ? n + 8 : n + n / 8; }
+
+template <bool WARP>
+__device__ __forceinline__ void fft_sync() {
+  if (WARP)
+    __syncwarp();
+  else
+    __syncthreads();
+}
 
 // One Stockham stage. FIRST: inputs from registers; LAST: outputs to registers.
-// sm: exchange buffer, element n at sm[xpad(n) * SS].
-template <int N, int E, int R, int NS, int DIR, int SS, bool FIRST, bool LAST>
+// sm: exchange buffer, element n at sm[xpad<SS>(n) * SS]. WARP: all T threads of the
+// FFT are in one warp, so __syncwarp orders the exchanges.
+template <int N, int E, int R, int NS, int DIR, int SS, bool WARP, bool FIRST, bool LAST>
 __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t,
                                                const float2* __restrict__ tw, int tws) {
   constexpr int T = N / E;
@@ -153,10 +166,10 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
     const int j = t + T * b;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      x[b][r] = FIRST ? v[b + r * BPT] : sm[xpad(j + r * (N / R)) * SS];
+      x[b][r] = FIRST ? v[b + r * BPT] : sm[xpad<SS>(j + r * (N / R)) * SS];
     }
   }
-  if (!FIRST && !LAST) __syncthreads();  // all reads done before the in-place writes
+  if (!FIRST && !LAST) fft_sync<WARP>();  // all reads done before the in-place writes
 #pragma unroll
   for (int b = 0; b < BPT; ++b) {
     const int j = t + T * b;
@@ -172,36 +185,38 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
     } else {
       const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[xpad(base + r * NS) * SS] = x[b][r];
+      for (int r = 0; r < R; ++r) sm[xpad<SS>(base + r * NS) * SS] = x[b][r];
     }
   }
-  if (!LAST) __syncthreads();
+  if (!LAST) fft_sync<WARP>();
 }
 
-template <int N, int E, int DIR, int SS, int S, bool DONE = (S >= Sched<N, E>::kStages)>
+template <int N, int E, int DIR, int SS, bool WARP, int S, bool DONE = (S >= Sched<N, E>::kStages)>
 struct Stages;
-template <int N, int E, int DIR, int SS, int S>
-struct Stages<N, E, DIR, SS, S, false> {
+template <int N, int E, int DIR, int SS, bool WARP, int S>
+struct Stages<N, E, DIR, SS, WARP, S, false> {
   using Sc = Sched<N, E>;
   static __device__ __forceinline__ void run(float2 (&v)[E], float2* sm, int t,
                                              const float2* __restrict__ tw, int tws) {
-    stockham_stage<N, E, Sc::radix(S), Sc::ns(S), DIR, SS, S == 0, S == Sc::kStages - 1>(v, sm, t, tw, tws);
-    Stages<N, E, DIR, SS, S + 1>::run(v, sm, t, tw, tws);
+    stockham_stage<N, E, Sc::radix(S), Sc::ns(S), DIR, SS, WARP, S == 0, S == Sc::kStages - 1>(v, sm, t, tw,
+                                                                                               tws);
+    Stages<N, E, DIR, SS, WARP, S + 1>::run(v, sm, t, tw, tws);
   }
 };
-template <int N, int E, int DIR, int SS, int S>
-struct Stages<N, E, DIR, SS, S, true> {
+template <int N, int E, int DIR, int SS, bool WARP, int S>
+struct Stages<N, E, DIR, SS, WARP, S, true> {
   static __device__ __forceinline__ void run(float2 (&)[E], float2*, int, const float2* __restrict__, int) {}
 };
 
-// N-point FFT by T = N/E threads; every thread of the CTA must call it (it contains
-// __syncthreads). v[e] holds element t + T*e on entry and on exit. tws: stride into
-// the twiddle table (table length / N). The exchange buffer is free on return
-// only after the caller's next __syncthreads.
-template <int N, int E, int DIR, int SS>
+// N-point FFT by T = N/E threads; every thread of the CTA (WARP = false) or of the
+// warp (WARP = true) must call it, since it synchronises between stages. v[e] holds
+// element t + T*e on entry and on exit. tws: stride into the twiddle table (table
+// length / N). The exchange buffer is free on return only after the caller's next
+// barrier of the same scope.
+template <int N, int E, int DIR, int SS, bool WARP = false>
 __device__ __forceinline__ void block_fft(float2 (&v)[E], float2* sm, int t,
                                           const float2* __restrict__ tw, int tws) {
-  Stages<N, E, DIR, SS, 0>::run(v, sm, t, tw, tws);
+  Stages<N, E, DIR, SS, WARP, 0>::run(v, sm, t, tw, tws);
 }
 
 // Elements per thread used for an N-point FFT.

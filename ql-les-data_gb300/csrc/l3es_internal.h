@@ -5,11 +5,104 @@
 
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include "../../include/l3es_gb300.h"
 #include "dns_kernels.cuh"
 
 namespace l3es {
+
+// Kernel kinds for the per-launch CUDA-event timer (l3es_plan_kernel_stats).
+enum KernelKind {
+  KK_X_INV = 0,     // kx_inv with curl prologue (6 fields)
+  KK_Y_INV,         // ky_pass inverse
+  KK_LINE_CROSS,    // line_cross
+  KK_Y_FWD,         // ky_pass forward (truncated)
+  KK_X_EPI,         // kx_fwd_band (band x-FFT + projection)
+  KK_BAND,          // k_band_scale
+  KK_FORCE,         // k_force_ekin
+  KK_X_INV_PLAIN,   // kx_inv without curl (irfftn)
+  KK_LINE_C2R,      // line_c2r
+  KK_LINE_R2C,      // line_r2c
+  KK_X_FWD_PLAIN,   // kx_fwd_plain (rfftn)
+  KK_REDUCE,        // energy / diagnostic reductions
+  KK_FILTER,        // spectral coarsening
+  KK_NUFFT_PREP,    // NUFFT deconvolve + pad
+  KK_NUFFT_FFT,     // NUFFT fine-grid FFT passes
+  KK_NUFFT_GATHER,  // NUFFT gather + advection
+  KK_PARTICLE_SORT, // particle binning
+  KK_RK_UPDATE,     // k_rk_update (elementwise RK4 combination)
+  KK_COUNT
+};
+const char* kernel_kind_name(int k);
+
+// Records an event pair around every launch while enabled; collect() sums the
+// elapsed times per kind after the work has finished.
+struct KTimer {
+  struct Rec {
+    int kind;
+    double bytes;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double ms[KK_COUNT] = {};
+  double bytes[KK_COUNT] = {};
+  long long launches[KK_COUNT] = {};
+  cudaEvent_t get() {
+    cudaEvent_t e;
+    if (!pool.empty()) {
+      e = pool.back();
+      pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
+  void start(int kind, double nbytes, cudaStream_t s) {
+    Rec r{kind, nbytes, get(), get()};
+    cudaEventRecord(r.a, s);
+    recs.push_back(r);
+  }
+  void stop(cudaStream_t s) { cudaEventRecord(recs.back().b, s); }
+  void collect() {
+    for (auto& r : recs) {
+      cudaEventSynchronize(r.b);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, r.a, r.b);
+      ms[r.kind] += t;
+      bytes[r.kind] += r.bytes;
+      launches[r.kind] += 1;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
+  void reset() {
+    collect();
+    for (int k = 0; k < KK_COUNT; ++k) {
+      ms[k] = 0.0;
+      bytes[k] = 0.0;
+      launches[k] = 0;
+    }
+  }
+  ~KTimer() {
+    for (auto& r : recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// Launch with optional per-kernel timing: kind, algorithmic bytes of the launch.
+#define L3ES_LAUNCH(ctx, kind, nbytes, stream, ...)                   \
+  do {                                                                \
+    ::l3es::KTimer* _tm = (ctx).timer;                                \
+    if (_tm) _tm->start((kind), (double)(nbytes), (stream));          \
+    __VA_ARGS__;                                                      \
+    if (_tm) _tm->stop(stream);                                       \
+  } while (0)
 
 // Geometry + scratch of one plan, handed to the per-N launch wrappers.
 struct Ctx {
@@ -21,18 +114,21 @@ struct Ctx {
   long long fs = 0;     // per field of the 6-field scratch W (== cs)
   long long ds = 0;     // per component of the nonlinear scratch DU (nmid*N*kt)
   long long ps = 0;     // real elements per physical component (N^dim)
-  int npartial = 0;     // CTAs of kx_fwd_epi per trajectory
+  int npartial = 0;     // CTAs of k_rk_update per trajectory (energy partial sums)
   float2* tw = nullptr;        // N-point twiddle table
   float2* W = nullptr;         // [batch][6][cs]
   float2* DU = nullptr;        // [batch][3][ds]
   float2* Tb = nullptr;        // [batch][3][cs] RK stage field
   float2* C = nullptr;         // [batch][3][cs] RK accumulator
+  float2* P = nullptr;         // [batch][3][pcs] projected nonlinear term on the kept band
+  long long pcs = 0;           // per component of P ((2kd+1)^(dim-1) * kt)
   double* partial = nullptr;   // [batch][npartial]
   double* band = nullptr;      // [batch] constant-power coefficient
   double* e0 = nullptr;        // [batch] ekin_tot targets
   double* einj = nullptr;      // [batch] scratch e_inj
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate
+  KTimer* timer = nullptr;     // per-launch timing (nullptr = off)
 };
 
 // Launch wrappers for one grid size N (both dims), explicitly instantiated per N.

@@ -1,0 +1,672 @@
+// Spectral coarsening, type-2 NUFFT interpolation to particles and periodic
+// advection (l3es/utils.py:100-138, l3es/integrator.py:21-91, l3es/combined.py:
+// 122-130, :199) for sm_103a.
+//
+// Data flow of one particle update (fused path of the combined loop):
+//   fine u_hat (N)  --k_crop-->  coarse half spectrum Hh (c)       [spectral_filtering]
+//   Hh --k_nufft_prep--> fine NUFFT grid G (n = 2c), deconvolved by the ES kernel's
+//   Fourier transform --3 c2c passes--> Re g (float) --k_nufft_gather--> u_r,
+//   advected r (particles binned by cell so warps gather neighbouring grid points)
+// and, when the coarse field itself is wanted, irfftn(Hh) at c (write_u / plots).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "dns_ops.cuh"
+#include "l3es_internal.h"
+
+namespace l3es {
+
+// ------------------------------------------------------------------------------
+// Coarse spectrum of spectral_filtering: Hh(f) = 0.5 (C(f) + conj C(p)), with
+// C(f) = U_fine(f) / (N/c)^dim on the crop set f in [-c/2, c/2-1]^dim and p the
+// crop-set representative of -f mod c. The half-average is fftn(real(ifftn(crop)))
+// (utils.py:126-127): it only changes modes with a component at -c/2.
+// Output: rfftn layout of the coarse grid, half axis index iz in [0, c/2].
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ int crop_freq(int i, int c) { return i < c / 2 ? i : i - c; }  // [-c/2, c/2)
+__device__ __forceinline__ int crop_wrap(int f, int c) {  // -> [-c/2, c/2)
+  f %= c;
+  if (f < -c / 2) f += c;
+  if (f >= c / 2) f -= c;
+  return f;
+}
+
+template <int DIM>
+__device__ __forceinline__ float2 fine_full(const float2* __restrict__ uh, int N, int fx, int fy, int fz) {
+  // full-spectrum value of the rfftn half spectrum at signed frequencies (3D: fx, fy,
+  // fz with fz on the half axis; 2D: fx, fy with fy on the half axis)
+  const int H = N / 2 + 1;
+  if (DIM == 3) {
+    if (fz >= 0) return __ldg(uh + ((long long)((fx + N) % N) * N + (fy + N) % N) * H + fz);
+    const float2 v = __ldg(uh + ((long long)((-fx + N) % N) * N + (-fy + N) % N) * H + (-fz));
+    return make_float2(v.x, -v.y);
+  } else {
+    if (fy >= 0) return __ldg(uh + (long long)((fx + N) % N) * H + fy);
+    const float2 v = __ldg(uh + (long long)((-fx + N) % N) * H + (-fy));
+    return make_float2(v.x, -v.y);
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_crop(const float2* __restrict__ uh, long long cs, int N, float2* __restrict__ hh, long long hcs, int c,
+       float scale) {
+  const int hc = c / 2 + 1;
+  const long long per = DIM == 3 ? (long long)c * c * hc : (long long)c * hc;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (i >= per) return;
+  int ix, iy, iz;
+  if (DIM == 3) {
+    iz = (int)(i % hc);
+    iy = (int)((i / hc) % c);
+    ix = (int)(i / ((long long)hc * c));
+  } else {
+    iz = 0;
+    iy = (int)(i % hc);
+    ix = (int)(i / hc);
+  }
+  const float2* u = uh + comp * cs;
+  float2 a, b;
+  if (DIM == 3) {
+    const int fx = crop_freq(ix, c), fy = crop_freq(iy, c), fz = iz < c / 2 ? iz : -c / 2;
+    a = fine_full<3>(u, N, fx, fy, fz);
+    b = fine_full<3>(u, N, crop_wrap(-fx, c), crop_wrap(-fy, c), crop_wrap(-fz, c));
+  } else {
+    const int fx = crop_freq(ix, c), fy = iy < c / 2 ? iy : -c / 2;
+    a = fine_full<2>(u, N, fx, fy, 0);
+    b = fine_full<2>(u, N, crop_wrap(-fx, c), crop_wrap(-fy, c), 0);
+  }
+  hh[comp * hcs + i] = make_float2(0.5f * scale * (a.x + b.x), 0.5f * scale * (a.y - b.y));
+}
+
+// ------------------------------------------------------------------------------
+// NUFFT grid: G(g) = Hhat(k) / (psi(kx) psi(ky) psi(kz)) at g = k mod n for k in
+// [-c/2, c/2-1]^dim (modes in fftshift order, as finufft receives them from
+// integrator.py:38-44), zero elsewhere. Hhat from the coarse half spectrum via
+// Hermitian symmetry. inv_psi: 1/psi_hat(k), k = -c/2..c/2-1.
+// ------------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_nufft_prep(const float2* __restrict__ hh, long long hcs, int c, const float* __restrict__ inv_psi,
+             float2* __restrict__ g, long long gcs, int n) {
+  const long long per = DIM == 3 ? (long long)n * n * n : (long long)n * n;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (i >= per) return;
+  int gx, gy, gz;
+  if (DIM == 3) {
+    gz = (int)(i % n);
+    gy = (int)((i / n) % n);
+    gx = (int)(i / ((long long)n * n));
+  } else {
+    gz = 0;
+    gy = (int)(i % n);
+    gx = (int)(i / n);
+  }
+  const int kx = gx < n / 2 ? gx : gx - n, ky = gy < n / 2 ? gy : gy - n, kz = gz < n / 2 ? gz : gz - n;
+  const int lo = -c / 2, hi = c / 2 - 1;
+  float2 out = make_float2(0.f, 0.f);
+  const bool in = kx >= lo && kx <= hi && ky >= lo && ky <= hi && (DIM == 2 || (kz >= lo && kz <= hi));
+  if (in) {
+    const int hc = c / 2 + 1;
+    const float2* h = hh + comp * hcs;
+    float2 v;
+    if (DIM == 3) {
+      if (kz >= 0) {
+        v = __ldg(h + ((long long)((kx + c) % c) * c + (ky + c) % c) * hc + kz);
+      } else {
+        const float2 t = __ldg(h + ((long long)((-kx + c) % c) * c + (-ky + c) % c) * hc + (-kz));
+        v = make_float2(t.x, -t.y);
+      }
+      const float s = inv_psi[kx + c / 2] * inv_psi[ky + c / 2] * inv_psi[kz + c / 2];
+      out = make_float2(v.x * s, v.y * s);
+    } else {
+      if (ky >= 0) {
+        v = __ldg(h + (long long)((kx + c) % c) * hc + ky);
+      } else {
+        const float2 t = __ldg(h + (long long)((-kx + c) % c) * hc + (-ky));
+        v = make_float2(t.x, -t.y);
+      }
+      const float s = inv_psi[kx + c / 2] * inv_psi[ky + c / 2];
+      out = make_float2(v.x * s, v.y * s);
+    }
+  }
+  g[comp * gcs + i] = out;
+}
+
+// ------------------------------------------------------------------------------
+// Last NUFFT grid pass: c2c inverse FFT of contiguous lines of n complex values,
+// writing only the real part (the interpolant of a real kernel needs no more).
+// ------------------------------------------------------------------------------
+template <int NL>
+__global__ void __launch_bounds__(128)
+line_c2c_re(const float2* __restrict__ g, float* __restrict__ gre, long long nlines, const float2* __restrict__ tw) {
+  constexpr int E = Fft<NL>::E, T = Fft<NL>::T;
+  static_assert(T <= 32, "line inside one warp");
+  constexpr int LPC = (32 / T) * 4;
+  constexpr int XS = xpad_len<1>(NL);
+  __shared__ float2 s_x[LPC * XS];
+  const int q = threadIdx.x / T, t = threadIdx.x % T;
+  const long long line_raw = (long long)blockIdx.x * LPC + q;
+  const bool valid = line_raw < nlines;
+  const long long line = valid ? line_raw : nlines - 1;
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = __ldg(g + line * NL + t + T * e);
+  block_fft<NL, E, kInv, 1, true>(v, s_x + q * XS, t, tw, 1);
+  if (valid) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) gre[line * NL + t + T * e] = v[e].x;
+  }
+}
+
+// ------------------------------------------------------------------------------
+// Particle binning by cell (counting sort) so that consecutive threads of the
+// gather work on neighbouring grid points. Bins: cubes of (n/nb)^dim fine cells.
+// ------------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ int particle_bin(const double* __restrict__ r, long long j, int nb) {
+  const double inv = nb / (2.0 * 3.14159265358979323846);
+  int b = 0;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    int cidx = (int)floor(r[j * DIM + d] * inv);
+    cidx = cidx < 0 ? 0 : (cidx >= nb ? nb - 1 : cidx);
+    b = b * nb + cidx;
+  }
+  return b;
+}
+
+template <int DIM>
+__global__ void k_bin_count(const double* __restrict__ r, long long np, int nb, int* __restrict__ count) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < np) atomicAdd(count + particle_bin<DIM>(r, j, nb), 1);
+}
+
+// exclusive scan of nbins counts by one CTA of 1024 threads (chunked)
+__global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ count, int nbins, int* __restrict__ start) {
+  __shared__ int part[1024];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nbins; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < nbins ? count[i] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int add = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < nbins) start[i] = carry + part[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += part[1023];
+    __syncthreads();
+  }
+}
+
+template <int DIM>
+__global__ void k_bin_scatter(const double* __restrict__ r, long long np, int nb, int* __restrict__ cursor,
+                              int* __restrict__ perm) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < np) perm[atomicAdd(cursor + particle_bin<DIM>(r, j, nb), 1)] = (int)j;
+}
+
+// ------------------------------------------------------------------------------
+// ES-kernel gather + Euler advection. For particle j (in binned order):
+//   u_r[j] = (1 / (n^dim c^dim)) sum_l Re g(l) prod_d phi((x_d/h - l_d) / (w/2))
+//   r_out[j] = (r[j] + dt u_r[j]) mod 2 pi                 (integrator.py:21-23)
+// phi(z) = exp(beta (sqrt(1 - z^2) - 1)); w-point support per axis.
+// ------------------------------------------------------------------------------
+template <int DIM, int W>
+__global__ void __launch_bounds__(128)
+k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, float beta, double norm,
+               const double* __restrict__ r, const int* __restrict__ perm, long long np, double* __restrict__ u_r,
+               double dt, double* __restrict__ r_out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const long long j = perm ? perm[i] : i;
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  const double h = two_pi / n;
+  float wk[DIM][W];
+  int id[DIM][W];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const double xs = r[j * DIM + d] / h;
+    const double l0 = ceil(xs - 0.5 * W);
+    const int il0 = (int)l0;
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
+      const float z = (float)((xs - (l0 + a)) / (0.5 * W));
+      const float q = 1.f - z * z;
+      wk[d][a] = q > 0.f ? expf(beta * (sqrtf(q) - 1.f)) : 0.f;
+      int g = (il0 + a) % n;
+      id[d][a] = g < 0 ? g + n : g;
+    }
+  }
+  double ur[3] = {0.0, 0.0, 0.0};
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const float* gc = gre + comp * gcs;
+    float acc = 0.f;
+    if (DIM == 3) {
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+        float sa = 0.f;
+#pragma unroll
+        for (int b = 0; b < W; ++b) {
+          const float* row = gc + ((long long)id[0][a] * n + id[1][b]) * n;
+          float sb = 0.f;
+#pragma unroll
+          for (int cc = 0; cc < W; ++cc) sb = fmaf(__ldg(row + id[DIM - 1][cc]), wk[DIM - 1][cc], sb);
+          sa = fmaf(sb, wk[1][b], sa);
+        }
+        acc = fmaf(sa, wk[0][a], acc);
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < W; ++a) {
+        const float* row = gc + (long long)id[0][a] * n;
+        float sb = 0.f;
+#pragma unroll
+        for (int b = 0; b < W; ++b) sb = fmaf(__ldg(row + id[1][b]), wk[1][b], sb);
+        acc = fmaf(sb, wk[0][a], acc);
+      }
+    }
+    ur[comp] = (double)acc * norm;
+  }
+  for (int comp = 0; comp < ncomp; ++comp) u_r[j * ncomp + comp] = ur[comp];
+  if (r_out) {
+    for (int d = 0; d < DIM; ++d) {
+      double x = r[j * DIM + d] + dt * ur[d];
+      x = x - two_pi * floor(x / two_pi);
+      if (x >= two_pi) x -= two_pi;  // Python % never returns the modulus itself
+      r_out[j * DIM + d] = x;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------
+// Exact spectral interpolation (interp_backend="dft", integrator.py:62-91):
+// u_r[j] = Re sum_{k in [-c/2, c/2-1]^dim} Hhat(k) exp(i k.x_j) / c^dim.
+// Separable: per (kx[, ky]) an inner sum over the last axis with per-thread phase
+// tables in shared memory (exp(i k x) by sincos in FP64 once per particle and mode).
+// ------------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(128)
+k_dft_interp(const float2* __restrict__ hh, long long hcs, int c, int ncomp, const double* __restrict__ r,
+             long long np, double* __restrict__ u_r, double dt, double* __restrict__ r_out) {
+  extern __shared__ float2 ph[];  // [DIM][c][128]
+  const long long j_raw = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j_raw < np;
+  const long long j = valid ? j_raw : 0;
+  const int tid = threadIdx.x;
+  for (int d = 0; d < DIM; ++d) {
+    const double x = r[j * DIM + d];
+    for (int k = 0; k < c; ++k) {
+      double s, co;
+      sincos((double)(k - c / 2) * x, &s, &co);
+      ph[(d * c + k) * 128 + tid] = make_float2((float)co, (float)s);
+    }
+  }
+  const int hc = c / 2 + 1;
+  double ur[3] = {0.0, 0.0, 0.0};
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const float2* h = hh + comp * hcs;
+    double tot = 0.0;
+    if (DIM == 3) {
+      for (int kx = -c / 2; kx < c / 2; ++kx) {
+        const float2 ex = ph[(0 * c + kx + c / 2) * 128 + tid];
+        float2 sx = make_float2(0.f, 0.f);
+        for (int ky = -c / 2; ky < c / 2; ++ky) {
+          float2 sy = make_float2(0.f, 0.f);
+          for (int kz = -c / 2; kz < c / 2; ++kz) {
+            float2 v;
+            if (kz >= 0) {
+              v = __ldg(h + ((long long)((kx + c) % c) * c + (ky + c) % c) * hc + kz);
+            } else {
+              const float2 t = __ldg(h + ((long long)((-kx + c) % c) * c + (-ky + c) % c) * hc - kz);
+              v = make_float2(t.x, -t.y);
+            }
+            const float2 ez = ph[(2 * c + kz + c / 2) * 128 + tid];
+            sy = make_float2(sy.x + v.x * ez.x - v.y * ez.y, sy.y + v.x * ez.y + v.y * ez.x);
+          }
+          const float2 ey = ph[(1 * c + ky + c / 2) * 128 + tid];
+          sx = make_float2(sx.x + sy.x * ey.x - sy.y * ey.y, sx.y + sy.x * ey.y + sy.y * ey.x);
+        }
+        tot += (double)sx.x * ex.x - (double)sx.y * ex.y;
+      }
+    } else {
+      for (int kx = -c / 2; kx < c / 2; ++kx) {
+        const float2 ex = ph[(0 * c + kx + c / 2) * 128 + tid];
+        float2 sy = make_float2(0.f, 0.f);
+        for (int ky = -c / 2; ky < c / 2; ++ky) {
+          float2 v;
+          if (ky >= 0) {
+            v = __ldg(h + (long long)((kx + c) % c) * hc + ky);
+          } else {
+            const float2 t = __ldg(h + (long long)((-kx + c) % c) * hc - ky);
+            v = make_float2(t.x, -t.y);
+          }
+          const float2 ey = ph[(1 * c + ky + c / 2) * 128 + tid];
+          sy = make_float2(sy.x + v.x * ey.x - v.y * ey.y, sy.y + v.x * ey.y + v.y * ey.x);
+        }
+        tot += (double)sy.x * ex.x - (double)sy.y * ex.y;
+      }
+    }
+    ur[comp] = tot / pow((double)c, DIM);
+  }
+  if (!valid) return;
+  for (int comp = 0; comp < ncomp; ++comp) u_r[j * ncomp + comp] = ur[comp];
+  if (r_out) {
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    for (int d = 0; d < DIM; ++d) {
+      double x = r[j * DIM + d] + dt * ur[d];
+      x = x - two_pi * floor(x / two_pi);
+      if (x >= two_pi) x -= two_pi;
+      r_out[j * DIM + d] = x;
+    }
+  }
+}
+
+// shift_fn(r, dr) = (r + scale * dr) mod box (integrator.py:21-23), elementwise
+__global__ void k_shift(const double* __restrict__ r, const double* __restrict__ dr, long long n, double scale,
+                        double box, double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = r[i] + scale * dr[i];
+  x = x - box * floor(x / box);
+  if (x >= box) x -= box;
+  out[i] = x;
+}
+
+}  // namespace l3es
+
+using namespace l3es;
+
+// ES kernel Fourier transform psi_hat(k) = (w / (2n)) int_{-1}^{1} phi(z) cos(pi k z w / n) dz
+// by Gauss-Legendre quadrature in FP64 (nodes from Newton iteration on P_m).
+static void gauss_legendre(int m, std::vector<double>& x, std::vector<double>& wt) {
+  x.resize(m);
+  wt.resize(m);
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < m; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (m + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= m; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      const double dp = m * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= m; ++k) {
+      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    const double dp = m * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = z;
+    wt[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+struct l3es_interp_plan {
+  int dim = 3, c = 32, n = 64, w = 6, n_fine = 0;
+  long long np_max = 0;
+  int nb = 16;  // bins per axis
+  double beta = 0.0;
+  float2* tw = nullptr;      // n-point twiddles
+  float2* hh = nullptr;      // [3][coarse half spectrum]
+  float2* g = nullptr;       // [3][n^dim]
+  float* gre = nullptr;      // [3][n^dim]
+  float* inv_psi = nullptr;  // [c]
+  int* count = nullptr;      // [nb^dim]
+  int* start = nullptr;      // [nb^dim]
+  int* perm = nullptr;       // [np_max]
+  l3es_plan* coarse = nullptr;  // size-c transforms (irfftn of Hh, rfftn of a coarse field)
+  long long hcs = 0, gcs = 0;
+  Ctx gctx;                  // geometry for the grid passes (twiddles only)
+  KTimer* timer = nullptr;
+  std::vector<void*> allocs;
+};
+
+static int ip_alloc(l3es_interp_plan* p, void** ptr, size_t bytes, const char* what) {
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(L3ES_ENOMEM, std::string("cudaMalloc(") + what + "): " + cudaGetErrorString(e));
+  }
+  p->allocs.push_back(*ptr);
+  return L3ES_OK;
+}
+
+static void ip_free(l3es_interp_plan* p) {
+  for (void* a : p->allocs) cudaFree(a);
+  p->allocs.clear();
+  if (p->coarse) l3es_plan_destroy(p->coarse);
+  p->coarse = nullptr;
+}
+
+// strided c2c passes of the NUFFT grid (inverse), via the ky_pass kernel
+template <int NG>
+static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
+  constexpr int TX = TW * Fft<NG>::T;
+  const long long per = p->gcs;
+  if (p->dim == 3) {
+    // x: pencils of stride n^2, columns = (y, z) flattened
+    ky_pass<NG, kInv><<<dim3((NG * NG + TW - 1) / TW, 1, 3), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
+    // y: pencils of stride n inside each x-plane, columns = z
+    ky_pass<NG, kInv><<<dim3((NG + TW - 1) / TW, NG, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+  } else {
+    ky_pass<NG, kInv><<<dim3((NG + TW - 1) / TW, 1, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+  }
+  const long long lines = 3 * per / NG;
+  constexpr int LPC = (32 / Fft<NG>::T) * 4;
+  line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->g, p->gre, lines, p->tw);
+}
+
+static int run_grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
+  switch (p->n) {
+    case 32: grid_passes<32>(p, s); return L3ES_OK;
+    case 64: grid_passes<64>(p, s); return L3ES_OK;
+    case 128: grid_passes<128>(p, s); return L3ES_OK;
+    case 256: grid_passes<256>(p, s); return L3ES_OK;
+    default: return fail(L3ES_EINVAL, "NUFFT grid size not supported");
+  }
+}
+
+extern "C" {
+
+int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width, int64_t np_max,
+                            l3es_interp_plan** out) {
+  if (!out) return fail(L3ES_EINVAL, "l3es_interp_plan_create: null out");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return fail(L3ES_EINVAL, "dim must be 2 or 3");
+  if (ckp_n != 16 && ckp_n != 32 && ckp_n != 64 && ckp_n != 128)
+    return fail(L3ES_EINVAL, "ckp_N must be 16, 32, 64 or 128");
+  if (n_fine != 0 && (n_fine < ckp_n || (n_fine & (n_fine - 1)) != 0))
+    return fail(L3ES_EINVAL, "ckp_N must be <= N (powers of two)");
+  if (width != 6 && width != 8 && width != 4) return fail(L3ES_EINVAL, "kernel width must be 4, 6 or 8");
+  if (np_max < 0) return fail(L3ES_EINVAL, "np_max < 0");
+  auto* p = new l3es_interp_plan();
+  p->dim = dim;
+  p->c = ckp_n;
+  p->n = 2 * ckp_n;
+  p->w = width;
+  p->n_fine = n_fine;
+  p->np_max = np_max;
+  p->beta = 2.30 * width;
+  p->nb = p->n / 4;
+  const int hc = ckp_n / 2 + 1;
+  p->hcs = dim == 3 ? (long long)ckp_n * ckp_n * hc : (long long)ckp_n * hc;
+  p->gcs = dim == 3 ? (long long)p->n * p->n * p->n : (long long)p->n * p->n;
+  const long long nbins = dim == 3 ? (long long)p->nb * p->nb * p->nb : (long long)p->nb * p->nb;
+  int rc = L3ES_OK;
+  rc = rc ? rc : ip_alloc(p, (void**)&p->tw, sizeof(float2) * p->n, "twiddles");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->hh, sizeof(float2) * 3 * p->hcs, "coarse spectrum");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->g, sizeof(float2) * 3 * p->gcs, "nufft grid");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->gre, sizeof(float) * 3 * p->gcs, "nufft grid re");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->inv_psi, sizeof(float) * ckp_n, "deconvolution");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->count, sizeof(int) * nbins, "bins");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * nbins, "bin starts");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * (np_max > 0 ? np_max : 1), "permutation");
+  if (rc == L3ES_OK) {
+    l3es_plan_desc d{};
+    d.dim = dim;
+    d.n = ckp_n;
+    d.batch = 1;
+    d.nu = 0.0;
+    d.dt = 1.0;
+    rc = l3es_plan_create(&d, &p->coarse);
+  }
+  if (rc != L3ES_OK) {
+    ip_free(p);
+    delete p;
+    return rc;
+  }
+  // host tables: n-point twiddles (FP64 -> FP32), 1/psi_hat(k) by quadrature
+  std::vector<float2> tw(p->n);
+  const double pi = 3.14159265358979323846;
+  for (int m = 0; m < p->n; ++m) {
+    const double a = -2.0 * pi * m / p->n;
+    tw[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  std::vector<double> zq, wq;
+  gauss_legendre(100, zq, wq);
+  std::vector<float> ipsi(ckp_n);
+  for (int i = 0; i < ckp_n; ++i) {
+    const double k = i - ckp_n / 2;
+    double sum = 0.0;
+    for (size_t q = 0; q < zq.size(); ++q) {
+      const double phi = std::exp(p->beta * (std::sqrt(1.0 - zq[q] * zq[q]) - 1.0));
+      sum += wq[q] * phi * std::cos(pi * k * zq[q] * width / p->n);
+    }
+    ipsi[i] = (float)(1.0 / ((double)width / (2.0 * p->n) * sum));
+  }
+  cudaError_t e = cudaMemcpy(p->tw, tw.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->inv_psi, ipsi.data(), sizeof(float) * ckp_n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    rc = cuda_check(e, "l3es_interp_plan_create");
+    ip_free(p);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return L3ES_OK;
+}
+
+int l3es_interp_plan_destroy(l3es_interp_plan* p) {
+  if (!p) return L3ES_OK;
+  ip_free(p);
+  delete p;
+  return L3ES_OK;
+}
+
+int l3es_interp_set_spectrum(l3es_interp_plan* p, const void* u_hat_fine, void* stream) {
+  if (!p || !u_hat_fine) return fail(L3ES_EINVAL, "l3es_interp_set_spectrum: null argument");
+  if (p->n_fine <= 0) return fail(L3ES_ESTATE, "plan was created without a fine grid (n_fine = 0)");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int N = p->n_fine, c = p->c;
+  const long long cs = p->dim == 3 ? (long long)N * N * (N / 2 + 1) : (long long)N * (N / 2 + 1);
+  const float scale = (float)std::pow((double)c / N, p->dim);
+  const unsigned blocks = (unsigned)((p->hcs + 255) / 256);
+  if (p->dim == 3)
+    k_crop<3><<<dim3(blocks, 3), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
+  else
+    k_crop<2><<<dim3(blocks, 3), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
+  return cuda_check(cudaGetLastError(), "l3es_interp_set_spectrum launch");
+}
+
+int l3es_interp_set_field(l3es_interp_plan* p, const float* u_coarse, void* stream) {
+  if (!p || !u_coarse) return fail(L3ES_EINVAL, "l3es_interp_set_field: null argument");
+  return l3es_rfftn(p->coarse, u_coarse, p->hh, stream);
+}
+
+int l3es_interp_coarse_field(l3es_interp_plan* p, float* u_coarse, void* stream) {
+  if (!p || !u_coarse) return fail(L3ES_EINVAL, "l3es_interp_coarse_field: null argument");
+  return l3es_irfftn(p->coarse, p->hh, u_coarse, stream);
+}
+
+int l3es_interp_coarse_spectrum(l3es_interp_plan* p, void* out, void* stream) {
+  if (!p || !out) return fail(L3ES_EINVAL, "l3es_interp_coarse_spectrum: null argument");
+  return cuda_check(cudaMemcpyAsync(out, p->hh, sizeof(float2) * 3 * p->hcs, cudaMemcpyDeviceToDevice,
+                                    (cudaStream_t)stream),
+                    "l3es_interp_coarse_spectrum");
+}
+
+int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, int32_t backend, double dt,
+                double* r_out, void* stream) {
+  if (!p || !r || !u_r) return fail(L3ES_EINVAL, "l3es_interp: null argument");
+  if (np < 0 || np > p->np_max) return fail(L3ES_EINVAL, "l3es_interp: np outside [0, np_max]");
+  if (backend != 0 && backend != 1) return fail(L3ES_EINVAL, "l3es_interp: backend must be 0 (nufft) or 1 (dft)");
+  if (np == 0) return L3ES_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int ncomp = p->dim;  // 3D: 3 velocity components; 2D: u, v (combined.py:122)
+  const unsigned pb = (unsigned)((np + 127) / 128);
+  if (backend == 1) {
+    const size_t smem = sizeof(float2) * p->dim * p->c * 128;
+    if (p->dim == 3) {
+      cudaFuncSetAttribute(k_dft_interp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dft_interp<3><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
+    } else {
+      cudaFuncSetAttribute(k_dft_interp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dft_interp<2><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
+    }
+    return cuda_check(cudaGetLastError(), "l3es_interp (dft) launch");
+  }
+  const unsigned gb = (unsigned)((p->gcs + 255) / 256);
+  if (p->dim == 3)
+    k_nufft_prep<3><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
+  else
+    k_nufft_prep<2><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
+  int rc = run_grid_passes(p, s);
+  if (rc != L3ES_OK) return rc;
+  const int nbins = p->dim == 3 ? p->nb * p->nb * p->nb : p->nb * p->nb;
+  rc = cuda_check(cudaMemsetAsync(p->count, 0, sizeof(int) * nbins, s), "l3es_interp memset");
+  if (rc != L3ES_OK) return rc;
+  if (p->dim == 3) {
+    k_bin_count<3><<<pb, 128, 0, s>>>(r, np, p->nb, p->count);
+    k_bin_scan<<<1, 1024, 0, s>>>(p->count, nbins, p->start);
+    k_bin_scatter<3><<<pb, 128, 0, s>>>(r, np, p->nb, p->start, p->perm);
+  } else {
+    k_bin_count<2><<<pb, 128, 0, s>>>(r, np, p->nb, p->count);
+    k_bin_scan<<<1, 1024, 0, s>>>(p->count, nbins, p->start);
+    k_bin_scatter<2><<<pb, 128, 0, s>>>(r, np, p->nb, p->start, p->perm);
+  }
+  const double norm = 1.0 / (std::pow((double)p->n, p->dim) * std::pow((double)p->c, p->dim));
+  const float beta = (float)p->beta;
+#define L3ES_GATHER(D, W)                                                                                   \
+  k_nufft_gather<D, W><<<pb, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
+                                          r_out)
+  if (p->dim == 3) {
+    if (p->w == 6) L3ES_GATHER(3, 6);
+    else if (p->w == 8) L3ES_GATHER(3, 8);
+    else L3ES_GATHER(3, 4);
+  } else {
+    if (p->w == 6) L3ES_GATHER(2, 6);
+    else if (p->w == 8) L3ES_GATHER(2, 8);
+    else L3ES_GATHER(2, 4);
+  }
+#undef L3ES_GATHER
+  return cuda_check(cudaGetLastError(), "l3es_interp launch");
+}
+
+int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box, double* out, void* stream) {
+  if (!r || !dr || !out) return fail(L3ES_EINVAL, "l3es_shift: null argument");
+  if (n <= 0) return n == 0 ? L3ES_OK : fail(L3ES_EINVAL, "l3es_shift: n < 0");
+  k_shift<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(r, dr, n, scale, box, out);
+  return cuda_check(cudaGetLastError(), "l3es_shift launch");
+}
+
+}  // extern "C"

@@ -12,6 +12,7 @@
 struct l3es_plan {
   l3es_plan_desc desc;
   l3es::Ctx ctx;
+  l3es::KTimer timer;
   l3es::DnsTable tab;
   int device = 0;
   long long ws_bytes = 0;
@@ -33,6 +34,14 @@ int cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return L3ES_OK;
   g_err = std::string(what) + ": " + cudaGetErrorString(e);
   return L3ES_ECUDA;
+}
+
+const char* kernel_kind_name(int k) {
+  static const char* names[KK_COUNT] = {
+      "kx_inv_curl", "ky_pass_inv", "line_cross", "ky_pass_fwd", "kx_fwd_band", "band_scale",
+      "force_ekin", "kx_inv", "line_c2r", "line_r2c", "kx_fwd", "reduce",
+      "filter", "nufft_prep", "nufft_fft", "nufft_gather", "particle_sort", "rk_update"};
+  return (k >= 0 && k < KK_COUNT) ? names[k] : "";
 }
 
 bool dns_table(int n, DnsTable* out) {
@@ -167,7 +176,8 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   c.fs = c.cs;
   c.ds = c.nmid * n * c.kt;
   c.ps = dim == 3 ? (long long)n * n * n : (long long)n * n;
-  c.npartial = ((c.h + TW - 1) / TW) * (int)c.nmid;
+  c.npartial = (int)((3 * c.cs / 2 + 255) / 256);
+  c.pcs = (long long)(2 * c.kd + 1) * (dim == 3 ? (2 * c.kd + 1) : 1) * c.kt;
   c.kf = desc->kf;
   c.eps_inj = desc->eps_inj;
   p->tab = tab;
@@ -179,6 +189,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.DU, sizeof(float2) * B * 3 * c.ds, "DU");
   rc = rc ? rc : plan_alloc(p, (void**)&c.Tb, sizeof(float2) * B * 3 * c.cs, "stage");
   rc = rc ? rc : plan_alloc(p, (void**)&c.C, sizeof(float2) * B * 3 * c.cs, "accumulator");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.P, sizeof(float2) * B * 3 * c.pcs, "band");
   rc = rc ? rc : plan_alloc(p, (void**)&c.partial, sizeof(double) * B * c.npartial, "partials");
   rc = rc ? rc : plan_alloc(p, (void**)&c.band, sizeof(double) * B, "band");
   rc = rc ? rc : plan_alloc(p, (void**)&c.e0, sizeof(double) * B, "e0");
@@ -220,6 +231,28 @@ int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count) {
 
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan) { return plan ? plan->ws_bytes : 0; }
 
+int l3es_plan_timing(l3es_plan* plan, int32_t enable) {
+  if (!plan) return fail(L3ES_EINVAL, "l3es_plan_timing: null plan");
+  plan->timer.reset();
+  plan->ctx.timer = enable ? &plan->timer : nullptr;
+  return cuda_check(cudaGetLastError(), "l3es_plan_timing");
+}
+
+int l3es_plan_kernel_stats(l3es_plan* plan, int32_t kind, double* total_ms, int64_t* launches,
+                           double* algo_bytes) {
+  if (!plan || !total_ms || !launches || !algo_bytes) return fail(L3ES_EINVAL, "l3es_plan_kernel_stats: null");
+  if (kind < 0 || kind >= KK_COUNT) return fail(L3ES_EINVAL, "l3es_plan_kernel_stats: bad kind");
+  plan->timer.collect();
+  *total_ms = plan->timer.ms[kind];
+  *launches = plan->timer.launches[kind];
+  *algo_bytes = plan->timer.bytes[kind];
+  return cuda_check(cudaGetLastError(), "l3es_plan_kernel_stats");
+}
+
+int32_t l3es_kernel_kind_count(void) { return KK_COUNT; }
+
+const char* l3es_kernel_kind_name(int32_t kind) { return kernel_kind_name(kind); }
+
 int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, void* stream) {
   if (!plan || !u_hat) return fail(L3ES_EINVAL, "l3es_step: null plan or u_hat");
   if (nsteps < 0) return fail(L3ES_EINVAL, "l3es_step: nsteps < 0");
@@ -248,11 +281,13 @@ int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
     if (d.forcing == L3ES_FORCING_EKIN_TOT) {
       if (c.dim == 3)
-        k_force_ekin<3><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf, inv_n2d,
-                                                eps64, einj, nullptr);
+        L3ES_LAUNCH(c, KK_FORCE, 0.0, s,
+                    k_force_ekin<3><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf,
+                                                            inv_n2d, eps64, einj, nullptr));
       else
-        k_force_ekin<2><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf, inv_n2d,
-                                                eps64, einj, nullptr);
+        L3ES_LAUNCH(c, KK_FORCE, 0.0, s,
+                    k_force_ekin<2><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf,
+                                                            inv_n2d, eps64, einj, nullptr));
     } else if (e_inj_dev) {
       L3ES_TRY_CUDA(cudaMemsetAsync(einj, 0, sizeof(double) * c.batch, s), "l3es_step memset");
     }
@@ -296,9 +331,11 @@ int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, voi
   const Ctx& c = plan->ctx;
   cudaStream_t s = (cudaStream_t)stream;
   const int nblk = (int)std::min<long long>(c.npartial, (c.cs + 255) / 256);
-  k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>((const float2*)u_hat, c.cs, c.h, nblk, c.partial);
+  L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
+              k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>((const float2*)u_hat, c.cs, c.h, nblk,
+                                                                   c.partial));
   const double scale = 0.5 / std::pow((double)c.n, 2 * c.dim);
-  k_sum_partials<<<c.batch, 256, 0, s>>>(c.partial, nblk, scale, out_dev);
+  L3ES_LAUNCH(c, KK_REDUCE, 0.0, s, k_sum_partials<<<c.batch, 256, 0, s>>>(c.partial, nblk, scale, out_dev));
   return cuda_check(cudaGetLastError(), "l3es_kinetic_energy launch");
 }
 

@@ -30,6 +30,20 @@ _SIGNATURES = {
     "l3es_rfftn": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_irfftn": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_kinetic_energy": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_plan_timing": (ctypes.c_int, [_P, _I]),
+    "l3es_plan_kernel_stats": (ctypes.c_int, [_P, _I, ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(ctypes.c_int64),
+                                              ctypes.POINTER(ctypes.c_double)]),
+    "l3es_kernel_kind_count": (ctypes.c_int32, []),
+    "l3es_kernel_kind_name": (ctypes.c_char_p, [_I]),
+    "l3es_interp_plan_create": (ctypes.c_int, [_I, _I, _I, _I, ctypes.c_int64, ctypes.POINTER(_P)]),
+    "l3es_interp_plan_destroy": (ctypes.c_int, [_P]),
+    "l3es_interp_set_spectrum": (ctypes.c_int, [_P, _P, _P]),
+    "l3es_interp_set_field": (ctypes.c_int, [_P, _P, _P]),
+    "l3es_interp_coarse_field": (ctypes.c_int, [_P, _P, _P]),
+    "l3es_interp_coarse_spectrum": (ctypes.c_int, [_P, _P, _P]),
+    "l3es_interp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
+    "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
     "l3es_last_error": (ctypes.c_char_p, []),
     "l3es_version": (ctypes.c_char_p, []),
 }
@@ -178,6 +192,21 @@ class Plan:
         _check(self._lib.l3es_kinetic_energy(self._h, _ptr(u_hat), _ptr(out), _stream(stream)),
                "l3es_kinetic_energy")
 
+    def timing(self, enable: bool) -> None:
+        """Start (clearing the counters) or stop per-launch CUDA-event timing."""
+        _check(self._lib.l3es_plan_timing(self._h, int(bool(enable))), "l3es_plan_timing")
+
+    def kernel_stats(self) -> dict:
+        """{kernel name: (launches, total ms, algorithmic bytes)} since timing(True)."""
+        out = {}
+        for k in range(self._lib.l3es_kernel_kind_count()):
+            ms, n, b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+            _check(self._lib.l3es_plan_kernel_stats(self._h, k, ctypes.byref(ms), ctypes.byref(n),
+                                                    ctypes.byref(b)), "l3es_plan_kernel_stats")
+            if n.value:
+                out[self._lib.l3es_kernel_kind_name(k).decode()] = (n.value, ms.value, b.value)
+        return out
+
     @property
     def workspace_bytes(self) -> int:
         return int(self._lib.l3es_plan_workspace_bytes(self._h))
@@ -199,3 +228,78 @@ def _prod(s):
     for v in s:
         p *= int(v)
     return p
+
+
+BACKENDS = {"nufft": 0, "dft": 1}
+
+
+class InterpPlan:
+    """Owns an ``l3es_interp_plan``: coarse spectrum, NUFFT grid, particle bins."""
+
+    def __init__(self, dim: int, ckp_n: int, n_fine: int = 0, width: int = 6, np_max: int = 0):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.l3es_interp_plan_create(int(dim), int(n_fine), int(ckp_n), int(width), int(np_max),
+                                           ctypes.byref(h)), "l3es_interp_plan_create")
+        self._h, self._lib = h, lib
+        self.dim, self.c, self.n_fine, self.width, self.np_max = int(dim), int(ckp_n), int(n_fine), int(width), int(np_max)
+
+    @property
+    def coarse_shape(self):
+        c = self.c
+        return (3, c, c, c) if self.dim == 3 else (3, c, c, 1)
+
+    @property
+    def coarse_spec_shape(self):
+        c = self.c
+        return (3, c, c, c // 2 + 1) if self.dim == 3 else (3, c, c // 2 + 1)
+
+    def set_spectrum(self, u_hat_fine, stream=None) -> None:
+        _check(self._lib.l3es_interp_set_spectrum(self._h, _ptr(u_hat_fine), _stream(stream)),
+               "l3es_interp_set_spectrum")
+
+    def set_field(self, u_coarse, stream=None) -> None:
+        if u_coarse.numel() != _prod(self.coarse_shape):
+            raise ValueError(f"expected float32 {self.coarse_shape}, got {tuple(u_coarse.shape)}")
+        _check(self._lib.l3es_interp_set_field(self._h, _ptr(u_coarse), _stream(stream)), "l3es_interp_set_field")
+
+    def coarse_field(self, out, stream=None) -> None:
+        if out.numel() != _prod(self.coarse_shape):
+            raise ValueError(f"expected float32 {self.coarse_shape}")
+        _check(self._lib.l3es_interp_coarse_field(self._h, _ptr(out), _stream(stream)), "l3es_interp_coarse_field")
+
+    def coarse_spectrum(self, out, stream=None) -> None:
+        _check(self._lib.l3es_interp_coarse_spectrum(self._h, _ptr(out), _stream(stream)),
+               "l3es_interp_coarse_spectrum")
+
+    def interp(self, r, u_r, backend: str = "nufft", dt: float = 0.0, r_out=None, stream=None) -> None:
+        import torch
+
+        if r.dtype != torch.float64 or u_r.dtype != torch.float64:
+            raise ValueError("positions and velocities are float64 (np, dim)")
+        if r.shape != u_r.shape or r.shape[-1] != self.dim:
+            raise ValueError(f"expected (np, {self.dim}) arrays")
+        _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend], float(dt),
+                                     _ptr(r_out), _stream(stream)), "l3es_interp")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.l3es_interp_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def shift(r, dr, scale: float = 1.0, box: float = 2 * 3.141592653589793, out=None, stream=None):
+    """shift_fn(r, scale * dr) on the GPU (float64 tensors); returns `out`."""
+    import torch
+
+    if out is None:
+        out = torch.empty_like(r)
+    _check(load().l3es_shift(_ptr(r), _ptr(dr), int(r.numel()), float(scale), float(box), _ptr(out),
+                             _stream(stream)), "l3es_shift")
+    return out

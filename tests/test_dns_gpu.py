@@ -151,3 +151,25 @@ def test_step3d_large_vs_oracle(n):
     p.step(uh, 1)
     assert _rel(uh.cpu().numpy(), uh_ref) < RTOL
     del rng
+
+
+@pytest.mark.parametrize("dim,n", [(2, 32), (2, 64), (3, 32)])
+def test_rhs_outside_dealias_band_is_viscous_only(dim, n):
+    """Modes outside the 2/3 cube only feel -nu k^2 u_hat (spectral_solver.py:56-59):
+    with nu = 0 the right-hand side there is exactly zero, for every component."""
+    rng = np.random.default_rng(n + dim)
+    shape = (3, n, n, n) if dim == 3 else (3, n, n, 1)
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    u = rng.standard_normal(shape)
+    uh = np.fft.rfftn(u, axes=axes).reshape((3, n, n, n // 2 + 1) if dim == 3 else (3, n, n // 2 + 1))
+    p = _plan(dim=dim, n=n, nu=0.0, dt=1e-3)
+    du = torch.full(p.spec_shape, float("nan"), dtype=torch.complex64, device="cuda")
+    p.rhs(_c64(uh), du)
+    d = du.cpu().numpy()
+    kd = max(k for k in range(n) if k < 2.0 / 3.0 * (n // 2 + 1))
+    kx = np.fft.fftfreq(n, 1.0 / n)
+    out_x = np.abs(kx) > kd
+    assert not np.isnan(d).any()
+    assert np.abs(d[:, out_x]).max() == 0.0
+    ref = R.rhs_wrapper(n, 0.0, axes)(u, uh, 1)
+    assert _rel(d, ref) < RTOL
