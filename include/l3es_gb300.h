@@ -148,6 +148,19 @@ int l3es_interp_coarse_spectrum(l3es_interp_plan* plan, void* out, void* stream)
 int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r,
                 int32_t backend, double dt, double* r_out, void* stream);
 
+/* Allocation-free form of l3es_interp_set_spectrum + l3es_interp(backend dft): no
+ * counterpart in the reference. For hosts that cannot let a library allocate
+ * device memory (e.g. a JAX/XLA FFI custom call, whose device memory belongs to
+ * XLA's preallocated pool). Coarsens the fine half spectrum u_hat_fine (N =
+ * n_fine) to ckp_N and evaluates the exact spectral interpolation at np particles
+ * r (float64, (np, dim)) into u_r (float64, (np, dim)). Its one scratch buffer is a
+ * fixed 417,792-byte array inside the library: ckp_N <= 32 in 3D, <= 64 in 2D,
+ * larger sizes return L3ES_EINVAL. Calls share that array, so calls that overlap
+ * on the GPU race; the first call on a device looks up the array's device address
+ * and should come before any stream capture on that device. */
+int l3es_interp_dft_noalloc(int32_t dim, int32_t n_fine, int32_t ckp_n, const void* u_hat_fine,
+                            const double* r, int64_t np, double* u_r, void* stream);
+
 /* shift_fn(r, scale * dr) = (r + scale * dr) mod box, elementwise over n doubles
  * (l3es/integrator.py:21-23). */
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,

@@ -44,6 +44,7 @@ _SIGNATURES = {
     "l3es_interp_coarse_spectrum": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
+    "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_last_error": (ctypes.c_char_p, []),
     "l3es_version": (ctypes.c_char_p, []),
 }
@@ -303,3 +304,16 @@ def shift(r, dr, scale: float = 1.0, box: float = 2 * 3.141592653589793, out=Non
     _check(load().l3es_shift(_ptr(r), _ptr(dr), int(r.numel()), float(scale), float(box), _ptr(out),
                              _stream(stream)), "l3es_shift")
     return out
+
+
+def interp_dft_noalloc(dim: int, n_fine: int, ckp_n: int, u_hat_fine, r, u_r, stream=None) -> None:
+    """Exact spectral interpolation from a fine spectrum without any device
+    allocation by the library (``l3es_interp_dft_noalloc``), for hosts that own all
+    device memory themselves. The caller provides every input and output tensor;
+    the library's fixed scratch limits ckp_n to 32 (3D) or 64 (2D)."""
+    import torch
+
+    if r.dtype != torch.float64 or u_r.dtype != torch.float64 or r.shape != u_r.shape:
+        raise ValueError("positions and velocities are float64 (np, dim)")
+    _check(load().l3es_interp_dft_noalloc(int(dim), int(n_fine), int(ckp_n), _ptr(u_hat_fine), _ptr(r),
+                                          int(r.shape[0]), _ptr(u_r), _stream(stream)), "l3es_interp_dft_noalloc")
