@@ -45,7 +45,7 @@ typedef struct l3es_plan l3es_plan;
  * e_kin_target, forcing_type) (l3es/spectral_solver.py:156-168) that the step needs. */
 typedef struct l3es_plan_desc {
   int32_t dim;        /* 2 or 3 (fft_axes (1,2) or (1,2,3)) */
-  int32_t n;          /* grid points per axis: 16, 32, 64, 128, 256 or 512 */
+  int32_t n;          /* grid points per axis: 8, 16, 32, 64, 128, 256 or 512 */
   int32_t batch;      /* independent trajectories stepped together (reference: 1) */
   int32_t forcing;    /* L3ES_FORCING_* */
   int32_t kf;         /* forcing band 0 < |k|^2 <= kf^2 (init_fields.py:167-188) */
@@ -71,6 +71,19 @@ int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count);
 
 /* Scratch bytes the plan holds on the device (for capacity planning). */
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
+
+/* Diagnostics of the drivers, FP64 results on the device (per trajectory):
+ * l3es_field_stats: out[4] = max|u_x|, max|u_y|, max|u_z|, 0.5 mean sum u^2 of a
+ *   physical field (spectral_solver.py:318-319; comp_dt at :123-127 follows from the
+ *   maxima: cfl / min_c(umax_c / dx + nu / dx^2));
+ * l3es_dissipation: out[1] = nu <|curl u|^2> of irfftn(i k x u_hat)
+ *   (utils.py:300-315), by Parseval on the half spectrum;
+ * l3es_energy_spectrum: ek[N] shell sums of |u_hat / N^dim|^2 * mul_fac over shells
+ *   int(|k| + 0.5), times 4 pi k^2 / (samples + eps) (utils.py:35-97). */
+int l3es_field_stats(l3es_plan* plan, const float* u, double* out_dev, void* stream);
+int l3es_dissipation(l3es_plan* plan, const void* u_hat, double nu, double* out_dev, void* stream);
+int l3es_energy_spectrum(l3es_plan* plan, const void* u_hat, double mul_fac, double* ek_dev,
+                         void* stream);
 
 /* Per-launch CUDA-event timing of the plan's kernels (tracing; the reference
  * only wall-clocks whole steps, spectral_solver.py:310-313). enable=1 clears the
@@ -119,7 +132,7 @@ typedef struct l3es_interp_plan l3es_interp_plan;
 /* Interpolator of spectral_interpolator_wrapper(ckp_N, fft_axes, splits, backend)
  * (l3es/integrator.py:26-34) plus the coarse grid of spectral_filtering
  * (l3es/utils.py:100-138). n_fine: grid of the spectra passed to
- * l3es_interp_set_spectrum (0 = coarse fields only); ckp_n: 16, 32, 64 or 128;
+ * l3es_interp_set_spectrum (0 = coarse fields only); ckp_n: 8, 16, 32, 64 or 128;
  * width: ES kernel width (4, 6 or 8; upsampling 2); np_max: particle capacity. */
 int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width,
                             int64_t np_max, l3es_interp_plan** out);

@@ -115,6 +115,7 @@ struct Ctx {
   long long ds = 0;     // per component of the nonlinear scratch DU (nmid*N*kt)
   long long ps = 0;     // real elements per physical component (N^dim)
   int npartial = 0;     // CTAs of k_rk_update per trajectory (energy partial sums)
+  long long partial_len = 0;  // doubles per trajectory in `partial`
   float2* tw = nullptr;        // N-point twiddle table
   float2* W = nullptr;         // [batch][6][cs]
   float2* DU = nullptr;        // [batch][3][ds]
@@ -122,7 +123,8 @@ struct Ctx {
   float2* C = nullptr;         // [batch][3][cs] RK accumulator
   float2* P = nullptr;         // [batch][3][pcs] projected nonlinear term on the kept band
   long long pcs = 0;           // per component of P ((2kd+1)^(dim-1) * kt)
-  double* partial = nullptr;   // [batch][npartial]
+  double* partial = nullptr;   // [batch][partial_len]: reduction partials, any layout of
+                               // at most partial_len doubles per trajectory
   double* band = nullptr;      // [batch] constant-power coefficient
   double* e0 = nullptr;        // [batch] ekin_tot targets
   double* einj = nullptr;      // [batch] scratch e_inj
@@ -145,6 +147,7 @@ struct DnsTable {
 template <int N>
 DnsTable make_dns_table();
 bool dns_table(int n, DnsTable* out);  // false if N is not compiled in
+const Ctx& plan_ctx(const l3es_plan* p);
 
 // thread-local error reporting
 void set_error(const std::string& msg);

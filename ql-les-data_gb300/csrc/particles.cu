@@ -332,6 +332,7 @@ static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
 
 static int run_grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
   switch (p->n) {
+    case 16: grid_passes<16>(p, s); return L3ES_OK;
     case 32: grid_passes<32>(p, s); return L3ES_OK;
     case 64: grid_passes<64>(p, s); return L3ES_OK;
     case 128: grid_passes<128>(p, s); return L3ES_OK;
@@ -347,8 +348,8 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   if (!out) return fail(L3ES_EINVAL, "l3es_interp_plan_create: null out");
   *out = nullptr;
   if (dim != 2 && dim != 3) return fail(L3ES_EINVAL, "dim must be 2 or 3");
-  if (ckp_n != 16 && ckp_n != 32 && ckp_n != 64 && ckp_n != 128)
-    return fail(L3ES_EINVAL, "ckp_N must be 16, 32, 64 or 128");
+  if (ckp_n != 8 && ckp_n != 16 && ckp_n != 32 && ckp_n != 64 && ckp_n != 128)
+    return fail(L3ES_EINVAL, "ckp_N must be 8, 16, 32, 64 or 128");
   if (n_fine != 0 && (n_fine < ckp_n || (n_fine & (n_fine - 1)) != 0))
     return fail(L3ES_EINVAL, "ckp_N must be <= N (powers of two)");
   if (width != 6 && width != 8 && width != 4) return fail(L3ES_EINVAL, "kernel width must be 4, 6 or 8");

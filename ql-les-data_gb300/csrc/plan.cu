@@ -44,8 +44,11 @@ const char* kernel_kind_name(int k) {
   return (k >= 0 && k < KK_COUNT) ? names[k] : "";
 }
 
+const Ctx& plan_ctx(const l3es_plan* p) { return p->ctx; }
+
 bool dns_table(int n, DnsTable* out) {
   switch (n) {
+    case 8: *out = make_dns_table<8>(); return true;
     case 16: *out = make_dns_table<16>(); return true;
     case 32: *out = make_dns_table<32>(); return true;
     case 64: *out = make_dns_table<64>(); return true;
@@ -151,7 +154,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   if (dim != 2 && dim != 3) return fail(L3ES_EINVAL, "dim must be 2 or 3, got " + std::to_string(dim));
   DnsTable tab;
   if (!dns_table(n, &tab))
-    return fail(L3ES_EINVAL, "N=" + std::to_string(n) + " not supported (16, 32, 64, 128, 256, 512)");
+    return fail(L3ES_EINVAL, "N=" + std::to_string(n) + " not supported (8, 16, 32, 64, 128, 256, 512)");
   if (desc->batch < 1) return fail(L3ES_EINVAL, "batch must be >= 1");
   if (!(desc->dt > 0.0) || !(desc->nu >= 0.0)) return fail(L3ES_EINVAL, "need dt > 0 and nu >= 0");
   if (desc->forcing < L3ES_FORCING_NONE || desc->forcing > L3ES_FORCING_CONST_POWER)
@@ -178,6 +181,9 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   c.ps = dim == 3 ? (long long)n * n * n : (long long)n * n;
   c.npartial = (int)((3 * c.cs / 2 + 255) / 256);
   c.pcs = (long long)(2 * c.kd + 1) * (dim == 3 ? (2 * c.kd + 1) : 1) * c.kt;
+  // room for the RK energy partials, the diagnostics' 608 blocks x 4 values and a
+  // 2 x N spectrum accumulator
+  c.partial_len = std::max<long long>(std::max<long long>(c.npartial, 4LL * 608), 2LL * n);
   c.kf = desc->kf;
   c.eps_inj = desc->eps_inj;
   p->tab = tab;
@@ -190,7 +196,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.Tb, sizeof(float2) * B * 3 * c.cs, "stage");
   rc = rc ? rc : plan_alloc(p, (void**)&c.C, sizeof(float2) * B * 3 * c.cs, "accumulator");
   rc = rc ? rc : plan_alloc(p, (void**)&c.P, sizeof(float2) * B * 3 * c.pcs, "band");
-  rc = rc ? rc : plan_alloc(p, (void**)&c.partial, sizeof(double) * B * c.npartial, "partials");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.partial, sizeof(double) * B * c.partial_len, "partials");
   rc = rc ? rc : plan_alloc(p, (void**)&c.band, sizeof(double) * B, "band");
   rc = rc ? rc : plan_alloc(p, (void**)&c.e0, sizeof(double) * B, "e0");
   rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");

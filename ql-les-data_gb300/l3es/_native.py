@@ -30,6 +30,9 @@ _SIGNATURES = {
     "l3es_rfftn": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_irfftn": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_kinetic_energy": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_field_stats": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_dissipation": (ctypes.c_int, [_P, _P, ctypes.c_double, _P, _P]),
+    "l3es_energy_spectrum": (ctypes.c_int, [_P, _P, ctypes.c_double, _P, _P]),
     "l3es_plan_timing": (ctypes.c_int, [_P, _I]),
     "l3es_plan_kernel_stats": (ctypes.c_int, [_P, _I, ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_int64),
@@ -192,6 +195,21 @@ class Plan:
         self._check_spec(u_hat)
         _check(self._lib.l3es_kinetic_energy(self._h, _ptr(u_hat), _ptr(out), _stream(stream)),
                "l3es_kinetic_energy")
+
+    def field_stats(self, u, out, stream=None) -> None:
+        """out (float64, 4 per trajectory): max|u_x|, max|u_y|, max|u_z|, kinetic energy."""
+        self._check_phys(u)
+        _check(self._lib.l3es_field_stats(self._h, _ptr(u), _ptr(out), _stream(stream)), "l3es_field_stats")
+
+    def dissipation(self, u_hat, nu, out, stream=None) -> None:
+        self._check_spec(u_hat)
+        _check(self._lib.l3es_dissipation(self._h, _ptr(u_hat), float(nu), _ptr(out), _stream(stream)),
+               "l3es_dissipation")
+
+    def energy_spectrum(self, u_hat, out, mul_fac: float = 1.0, stream=None) -> None:
+        self._check_spec(u_hat)
+        _check(self._lib.l3es_energy_spectrum(self._h, _ptr(u_hat), float(mul_fac), _ptr(out), _stream(stream)),
+               "l3es_energy_spectrum")
 
     def timing(self, enable: bool) -> None:
         """Start (clearing the counters) or stop per-launch CUDA-event timing."""

@@ -1,0 +1,99 @@
+"""DNS + Lagrangian particles driver: drop-in for l3es/combined.py.
+
+Same keyword set and loop order as the reference (combined.py:18-219): at every step
+the DNS advances, the field is coarsened to ckp_N, the particle velocity is
+interpolated from it at the positions from before the step's advection, and the
+particles move by an explicit Euler shift. On the GPU the coarsening is taken
+directly from the fine spectrum and the interpolation and shift are fused
+(l3es_interp_set_spectrum + l3es_interp with r_out).
+
+Outside this package: SPH relaxation (relax_dt_factor > 0 raises), the SPH density
+column (written empty) and plots. Particle checkpoints go to step_XXXXX.npz files
+with the reference's keys r and u (the reference writes h5 through JAX-SPH).
+"""
+
+from __future__ import annotations
+
+import csv
+import os
+from time import time
+
+import numpy as np
+
+from .integrator import set_up_integrator
+from .spectral_solver import _field_stats, dt_from_stats, set_up_solver, _torch
+from .utils import _interp_plan, write_u
+
+
+def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, u_ref=4.0, ckp_N=64,
+             state_0_path=None, interp_backend="dft", relax_dt_factor=0.0, dft_splits=8, seed=42, rejit=True,
+             forcing_type="none", e_kin_target=None, kf=None, log_freq=100, vis_freq=100, ckp_freq=100,
+             dst_path=None, **ext):
+    """Integrate particles along the DNS velocity (combined.py:18-219). Returns the final
+    (u, u_hat, r)."""
+    if relax_dt_factor and relax_dt_factor > 0.0:
+        raise NotImplementedError("SPH relaxation (relax_dt_factor > 0) is not part of this package")
+    torch = _torch()
+    dst_path = dst_path or "results"
+    int_path = os.path.join(dst_path, "com")
+    os.makedirs(int_path, exist_ok=True)
+    diagnostics_path = os.path.join(dst_path, "diagnostics.csv")
+    with open(diagnostics_path, "w", newline="") as f:
+        csv.writer(f).writerow(["step", "time", "umax", "ekin", "dt_est", "e_inj", "rho_max"])
+
+    u, u_hat, xyz_vis, dx_dns, integrate_fn, L, fft_axes, ek_ini, e_inj = set_up_solver(
+        N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target, forcing_type, rejit, **ext)
+    print(f"{'#' * 79}\nSimulation with N={N}, nu={nu}, t_final={t_final}, dt={dt}",
+          f"E_kin_init={ek_ini:.3f}\n{'#' * 79}")
+    r, _, _, _, _, _, _ = set_up_integrator(state_0_path, dim, ckp_N, dft_splits, u_ref, interp_backend)
+    npart = r.shape[0]
+    ip = _interp_plan(dim, N, ckp_N, np_max=npart)
+    u_r = torch.empty_like(r)
+    r_next = torch.empty_like(r)
+    e_acc = torch.zeros((), dtype=torch.float64, device="cuda")
+
+    t_sim, t_int, t0 = 0.0, 0.0, time()
+    tstep_max = round(t_final / dt)
+    burnin_steps = round(t_burnin / dt) if t_burnin > 0 else 0
+    for i in range(tstep_max + 1):
+        if i == burnin_steps:
+            write_u(u, i, dst_path, N, suffix="_burnin")
+        if i == burnin_steps and case == "HIT":
+            _, _, _, _, integrate_fn, _, _, _, _ = set_up_solver(
+                N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target, "none", rejit, **ext)
+        t_temp = time()
+        u, u_hat, e_inj = integrate_fn(u, u_hat)
+        torch.cuda.synchronize()
+        t_sim += time() - t_temp
+        e_acc += e_inj
+
+        t_temp = time()
+        # u_lres = spectral_filtering(u_hres, ckp_N); u_r = interpolator(u_lres, r);
+        # r_next = shift_fn(r, dt * u_r)   (combined.py:122-130, :199)
+        ip.set_spectrum(u_hat)
+        ip.interp(r, u_r, backend=interp_backend, dt=dt, r_out=r_next)
+        torch.cuda.synchronize()
+        t_int += time() - t_temp
+
+        is_ckp = (i % ckp_freq == 0) and (i >= burnin_steps)
+        if i % log_freq == 0:
+            st = _field_stats(u, dim).cpu().numpy()
+            umax, e_kin = float(st[:3].max()), float(st[3])
+            dt_est = float(dt_from_stats(st, dx_dns, nu))
+            with open(diagnostics_path, "a", newline="") as f:
+                csv.writer(f).writerow([i, float(i * dt), umax, e_kin, dt_est, float(e_inj), ""])
+            print(f"Step {i}/{tstep_max}, u_max = {umax:.3f}, E_kin = {e_kin:.3f}, "
+                  f"dt_est = {dt_est:.5f}, E_inj = {float(e_inj):.3f}")
+        if is_ckp:
+            np.savez(os.path.join(int_path, f"step_{i:05d}.npz"), r=r.cpu().numpy(), u=u_r.cpu().numpy())
+        r, r_next = r_next, r
+
+    if case == "HIT" and forcing_type != "none" and tstep_max > 0:
+        avg = float(e_acc) / tstep_max
+        if avg > 0:
+            tau = 1.0 / (avg * kf**2) ** (1 / 3)
+            print(f"Eddy turnover time =            {tau:.3f}")
+            print(f"Number of eddy turnover times = {t_final / tau:.3f}")
+            print(f"Average energy injected =       {avg:.3f}")
+    print(f"t_tot = {time() - t0:.3f}, t_sim = {t_sim}, t_int = {t_int:.3f}")
+    return u, u_hat, r

@@ -122,7 +122,8 @@ def init_u_random2d(N, seed=0, kmax=8.0, energy=0.5, target_dim=3):
     kk = np.sqrt(kx * kx + ky * ky)
     phase = rng.uniform(0.0, 2.0 * np.pi, size=kk.shape)
     psi = np.where((kk > 0) & (kk <= kmax), np.exp(1j * phase), 0.0)
-    uv = np.stack([np.fft.irfftn(1j * ky * psi, s=(N, N)), np.fft.irfftn(-1j * kx * psi, s=(N, N))])
+    uv = np.stack([np.fft.irfftn(1j * ky * psi, s=(N, N), axes=(0, 1)),
+                   np.fft.irfftn(-1j * kx * psi, s=(N, N), axes=(0, 1))])
     uv *= np.sqrt(energy / (0.5 * np.mean(np.sum(uv * uv, axis=0))))
     if target_dim == 3:
         uv = np.concatenate([uv[..., None], np.zeros((1, N, N, 1))], axis=0)
