@@ -43,6 +43,22 @@ CKP_N = 32
 WITH_PARTICLES = True  # coarsening + NUFFT + advection inside the step
 
 
+def _ncu_traffic(kernel: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu --set full
+    summary of the 256^3 stage (profiles/ncu_full_hit256_stage.md), or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_full_hit256_stage.md")
+    if not os.path.exists(p):
+        return None
+    names = {"line_cross": "line_cross<256>", "ky_pass_inv": "ky_pass<256, 1>", "kx_inv_curl": "kx_inv<256, 3, 1>",
+             "rk_update": "k_rk_update<256, 3>", "kx_fwd_band": "kx_fwd_band<256, 3>", "ky_pass_fwd": "ky_pass<256, -1>"}
+    want = names.get(kernel)
+    for line in open(p):
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if want and cells and cells[0] == want:
+            return (float(cells[2]) + float(cells[3])) * 1e6
+    return None
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -215,6 +231,7 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
         return acc
 
     uh = torch.fft.rfftn(torch.from_numpy(u0).to(dev), dim=axes)
+    step(uh.clone())  # creates the cuFFT plans outside the timed region (result discarded)
     for _ in range(warmup):
         uh = step(uh)
     torch.cuda.synchronize()
@@ -225,6 +242,7 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    # kinetic energy by Parseval on the half spectrum, FP64
     ke = 0.5 * float((wts * (uh.abs() ** 2).sum(0)).sum()) / float(n) ** 6
     return 1e3 / ms, ke
 
@@ -342,13 +360,29 @@ def run_ours(args):
     h2d = npart * 3 * 8
     d2h = 2 * npart * 3 * 8 + 8
 
+    # accuracy clause of the metric: kinetic energy of the FP32 step after K steps vs
+    # the FP64 plain form from the same initial field (which also times the comparator)
+    ke_check = None
+    fp64_rate = None
+    if rank == 0 and not args.skip_baselines and args.ke_steps > 0:
+        uh_chk = uh0.clone()
+        plan.step(uh_chk, args.ke_steps)
+        ke_dev2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        plan.kinetic_energy(uh_chk, ke_dev2)
+        ke32 = float(ke_dev2)
+        fp64_rate, ke64 = fp64_plain_rate(u0, dt, n, steps=args.ke_steps, warmup=0)
+        ke_check = {"steps": args.ke_steps, "ke_fp32": ke32, "ke_fp64": ke64,
+                    "rel_err": abs(ke32 - ke64) / ke64, "criterion": 1e-5}
+        del uh_chk
+
     line = None
     if rank == 0 and args.skip_baselines:
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "ms_per_step": ms,
                 "note": "--skip-baselines (profiling run): no comparator, CPU or e2e legs"}
     elif rank == 0:
-        # FP64 plain comparator (a few steps) and the CPU baseline sample
-        fp64_rate, _ = fp64_plain_rate(u0, dt, n, steps=max(2, min(args.steps, 5)), warmup=1)
+        # FP64 plain comparator (timed by the KE check, else a few steps) and the CPU sample
+        if fp64_rate is None:
+            fp64_rate, _ = fp64_plain_rate(u0, dt, n, steps=max(2, min(args.steps, 5)), warmup=1)
         cpu_rate, cores = cpu_step_rate(n, 1, 0, u0=u0, dt=dt)
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -360,10 +394,12 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "1 gpu",
                        "l2": "working set (~1.3 GB) larger than L2, no flush"},
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": _ncu_traffic(name),
                          "algo_bytes_per_launch": tb / nl, "ms_per_launch": tms / nl},
             "kernels": kernels,
-            "fp64_plain": {"value": fp64_rate, "unit": "steps/s", "speedup": value / world / fp64_rate},
+            "fp64_plain": {"value": fp64_rate, "unit": "steps/s", "speedup": value / world / fp64_rate,
+                           "note": "reference algorithm restated with torch.fft (cuFFT) in complex128, same GPU"},
+            "ke_check": ke_check,
             "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": f"1 step at {n}^3 (RK4 + filter + NUFFT + advection), FP64 NumPy/SciPy"},
             "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -387,6 +423,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--ke-steps", type=int, default=200,
+                    help="steps of the FP32-vs-FP64 kinetic energy check (0 = skip)")
     ap.add_argument("--skip-baselines", action="store_true",
                     help="profiling runs: time our step only (no FP64 plain, CPU or e2e legs)")
     args = ap.parse_args()
