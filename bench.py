@@ -377,7 +377,7 @@ def run_ours(args):
 
     line = None
     if rank == 0 and args.skip_baselines:
-        line = {"metric": METRIC, "value": value, "unit": "steps/s", "ms_per_step": ms,
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "ms_per_step": ms, "kernels": kernels,
                 "note": "--skip-baselines (profiling run): no comparator, CPU or e2e legs"}
     elif rank == 0:
         # FP64 plain comparator (timed by the KE check, else a few steps) and the CPU sample

@@ -11,7 +11,7 @@ tumaer/ql-les-data project). Parity is pinned by the reference's own golden valu
 0.124953117517) and by fixtures generated from the reference's own runnable NumPy
 solver (``tests/golden/make_golden.py``).
 
-Terms that BASELINE-style workloads ask for but the reference does not have
+Terms that the benchmark workloads need but the reference does not have
 (linear drag, Kolmogorov forcing, constant-power band forcing, the
 k^4 exp(-2(k/kp)^2) Rogallo spectrum, band-limited random 2D init) are opt-in
 arguments that default to the reference behaviour.

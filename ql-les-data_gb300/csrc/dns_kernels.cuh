@@ -14,6 +14,7 @@
 //                stored only for the kept (dealiased) half-axis modes
 //   ky_pass      y-axis forward c2c (3D only), stored only for kept ky rows
 //   kx_fwd_band  x-axis forward c2c on the kept band, dealias mask, Leray projection
+//                (and the constant-power band coefficient of the stage field)
 //   k_rk_update  elementwise viscosity, extension terms and RK4 stage combination
 // Intermediate fields never exist in physical space in HBM.
 #pragma once
@@ -29,14 +30,26 @@ constexpr int TW = 8;  // pencils (columns) per CTA in the strided x / y passes
 // independently. 4 warps per CTA.
 template <int N>
 struct LineCfg {
-  static constexpr int M = N / 2;                 // half-length complex FFT
+  static constexpr int M = N / 2;                          // half-length complex FFT
+  // radix 8: at 16 values per thread the 3 cross-product accumulators spill (measured
+  // 224 us vs 193 us per 256^3 launch), so the line passes keep two exchanges
   static constexpr int E = Fft<M>::E;
-  static constexpr int T = Fft<M>::T;             // threads per line
+  static constexpr int T = M / E;                          // threads per line
   static_assert(T <= 32, "line passes need the line inside one warp (N <= 512)");
-  static constexpr int LPW = 32 / T;              // lines per warp
+  static constexpr int LPW = 32 / T;                       // lines per warp
   static constexpr int THREADS = 128;
-  static constexpr int LPC = LPW * (THREADS / 32);  // lines per CTA
-  static constexpr int XS = xpad_len<1>(M);       // exchange slots per line
+  static constexpr int LPC = LPW * (THREADS / 32);         // lines per CTA
+  static constexpr int XS = xpad_len<1>(M);                // exchange slots per line
+};
+
+// y-axis pass tiling: radix 16 (one exchange at N = 256) on 16-column tiles where the
+// shared-memory tile fits the static limit.
+template <int N>
+struct KyCfg {
+  static constexpr int E = N >= 128 ? 16 : Fft<N>::E;
+  static constexpr int TWY = (N >= 128 && N <= 256) ? 16 : 8;
+  static constexpr int T = N / E;
+  static constexpr int THREADS = TWY * T;
 };
 
 // wavenumber vector (reference kkk, spectral_solver.py:32-39): 3D (kx, kmid, khalf),
@@ -115,19 +128,20 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
 // are written (forward pass truncated to the dealiased band; kd_store = N/2 keeps all).
 // ------------------------------------------------------------------------------
 template <int N, int DIR>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
+__global__ void __launch_bounds__(KyCfg<N>::THREADS)
 ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
         const float2* __restrict__ tw) {
-  constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int col = blockIdx.x * TW + p;
+  using C = KyCfg<N>;
+  constexpr int E = C::E, T = C::T, TWY = C::TWY;
+  __shared__ float2 sm[xpad_len<TWY>(N) * TWY];
+  const int p = threadIdx.x % TWY, t = threadIdx.x / TWY;
+  const int col = blockIdx.x * TWY + p;
   const bool ok = col < ncols;
   float2* base = w + blockIdx.z * fs + (long long)blockIdx.y * N * row + col;
   float2 v[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) v[e] = ok ? base[(long long)(t + T * e) * row] : make_float2(0.f, 0.f);
-  block_fft<N, E, DIR, TW>(v, sm + p, t, tw, 1);
+  block_fft<N, E, DIR, TWY>(v, sm + p, t, tw, 1);
   if (ok) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -181,10 +195,11 @@ __device__ __forceinline__ void c2r_load_pack(const float2* __restrict__ X, int 
 
 // M-point forward FFT output Z (exchange buffer, padded index) -> r2c value X[k],
 // k in [0, M] (Z is M-periodic; W^M = -1 gives X[M] = Re Z0 - Im Z0).
+template <int E>
 __device__ __forceinline__ float2 r2c_unpack(const float2* Z, int k, int M,
                                              const float2* __restrict__ twN) {
-  const float2 zk = Z[xpad<1>(k < M ? k : 0)];
-  const float2 zm = Z[xpad<1>(k == 0 ? 0 : M - k)];
+  const float2 zk = Z[xpad<1, E>(k < M ? k : 0)];
+  const float2 zm = Z[xpad<1, E>(k == 0 ? 0 : M - k)];
   const float2 s = make_float2(zk.x + zm.x, zk.y - zm.y);
   const float2 d = make_float2(zk.x - zm.x, zk.y + zm.y);
   const float2 id = mul_i<kFwd>(cmul(__ldg(twN + k), d));  // -i W^k d
@@ -259,11 +274,11 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
     block_fft<M, E, kFwd, 1, true>(cr[c], xs, t, twN, 2);
     __syncwarp();
 #pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad<1>(t + T * e)] = cr[c][e];
+    for (int e = 0; e < E; ++e) xs[xpad<1, E>(t + T * e)] = cr[c][e];
     __syncwarp();
     if (valid) {
       float2* dst = db + c * ds;
-      for (int k = t; k < kt; k += T) dst[k] = k <= kd ? r2c_unpack(xs, k, M, twN) : make_float2(0.f, 0.f);
+      for (int k = t; k < kt; k += T) dst[k] = k <= kd ? r2c_unpack<E>(xs, k, M, twN) : make_float2(0.f, 0.f);
     }
     __syncwarp();
   }
@@ -325,11 +340,11 @@ line_r2c(const float* __restrict__ in, long long is, float2* __restrict__ w, lon
     block_fft<M, E, kFwd, 1, true>(v, xs, t, twN, 2);
     __syncwarp();
 #pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad<1>(t + T * e)] = v[e];
+    for (int e = 0; e < E; ++e) xs[xpad<1, E>(t + T * e)] = v[e];
     __syncwarp();
     if (valid) {
       float2* dst = w + (long long)batch * 3 * fs + f * fs + line * H;
-      for (int k = t; k < H; k += T) dst[k] = r2c_unpack(xs, k, M, twN);
+      for (int k = t; k < H; k += T) dst[k] = r2c_unpack<E>(xs, k, M, twN);
     }
     __syncwarp();
   }
@@ -362,6 +377,62 @@ kx_fwd_plain(const float2* __restrict__ w, long long fs, float2* __restrict__ uh
       for (int e = 0; e < E; ++e) uh[bu + c * cs + (long long)(t + T * e) * MC + m] = v[e];
     }
     __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------
+// Low-wavenumber band helpers (few hundred modes; one CTA per trajectory).
+// band: 0 < |k|^2 <= kf^2 (init_fields.py:167-188). weights: half-axis multiplicity.
+// ------------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ bool band_mode(int i, int N, int kf, long long& idx, int& wgt) {
+  // enumerate kx in [-kf, kf], (3D) km in [-kf, kf], kh in [0, kf]
+  const int n1 = 2 * kf + 1, nh = kf + 1;
+  const int kh = i % nh;
+  const int r = i / nh;
+  const int km = DIM == 3 ? (r % n1) - kf : 0;
+  const int kx = DIM == 3 ? (r / n1) - kf : r - kf;
+  const int k2 = kx * kx + km * km + kh * kh;
+  if (k2 == 0 || k2 > kf * kf) return false;
+  const int H = N / 2 + 1;
+  const int xi = kx < 0 ? kx + N : kx;
+  const int mi = km < 0 ? km + N : km;
+  idx = DIM == 3 ? ((long long)xi * N + mi) * H + kh : (long long)xi * H + kh;
+  wgt = (kh == 0 || kh == N / 2) ? 1 : 2;
+  return true;
+}
+
+template <int DIM>
+__device__ __forceinline__ int band_count(int kf) {
+  return DIM == 3 ? (2 * kf + 1) * (2 * kf + 1) * (kf + 1) : (2 * kf + 1) * (kf + 1);
+}
+
+// Constant-power band forcing coefficient eps / (2 E_f + tiny) of a stage field
+// (extension), computed by all threads of one block; thread 0 stores it.
+template <int DIM>
+__device__ __forceinline__ void band_coefficient(const float2* __restrict__ ub, long long cs, int N, int kf,
+                                                 double inv_n2d, double eps_inj, double tiny, double* out) {
+  __shared__ double red_band[32];
+  double lo = 0.0;
+  const int nb = band_count<DIM>(kf);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    long long idx;
+    int wg;
+    if (!band_mode<DIM>(i, N, kf, idx, wg)) continue;
+    for (int c = 0; c < 3; ++c) {
+      const float2 v = ub[c * cs + idx];
+      lo += wg * ((double)v.x * v.x + (double)v.y * v.y);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) lo += __shfl_xor_sync(0xffffffffu, lo, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red_band[wid] = lo;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double L = 0.0;
+    for (int i = 0; i < nw; ++i) L += red_band[i];
+    *out = eps_inj / (2.0 * (0.5 * L * inv_n2d) + tiny);
   }
 }
 
@@ -404,7 +475,8 @@ __device__ __forceinline__ void block_sum_store(double v, double* partial, int b
 template <int N, int DIM>
 __global__ void __launch_bounds__(TW * Fft<N>::T)
 kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
-            const float2* __restrict__ tw) {
+            const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
+            double inv_n2d, double eps_inj, double* __restrict__ band_scale) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
   constexpr int NMID = DIM == 3 ? N : 1;
   __shared__ float2 sm[xpad_len<TW>(N) * TW];
@@ -416,6 +488,9 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
   const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
   const int batch = blockIdx.z;
   const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
+  if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
+    band_coefficient<DIM>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30,
+                          band_scale + batch);
   float2 d[3][E];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
@@ -458,13 +533,14 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
 // Every thread loads all its operands before storing (us/out and acc alias).
 // ------------------------------------------------------------------------------
 template <int N, int DIM>
-__device__ __forceinline__ float2 rk_elem(long long i, int c, float2 sv, float2 a0, float2 z0,
+__device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a0, float2 z0,
                                           const float2* __restrict__ P, long long pcs, int kt, int kd,
                                           const EpiParams& prm, float fscale, float2& nv, double& esum) {
-  constexpr int H = N / 2 + 1;
-  constexpr int NMID = DIM == 3 ? N : 1;
+  // i < 3 N^2 (N/2+1) < 2^31 for N <= 512: 32-bit division by compile-time constants
+  constexpr unsigned H = N / 2 + 1;
+  constexpr unsigned NMID = DIM == 3 ? N : 1;
   const int kh = (int)(i % H);
-  const long long rest = i / H;
+  const unsigned rest = i / H;
   const int mid = (int)(rest % NMID);
   const int kxi = (int)(rest / NMID);
   const int kx = kfull(kxi, N);
@@ -530,10 +606,11 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
     if (prm.rk > 0 && prm.rk < 3) z4 = reinterpret_cast<const float4*>(u0 + bo)[q];
     const float2* Pb = P + (long long)batch * 3 * pcs;
     float2 nv0, nv1;
-    const int c0 = (int)(g / cs), c1 = (int)((g + 1) / cs);
-    const float2 r0 = rk_elem<N, DIM>(g - (long long)c0 * cs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
+    const unsigned ucs = (unsigned)cs, ug = (unsigned)g;
+    const int c0 = (int)(ug / ucs), c1 = (int)((ug + 1u) / ucs);
+    const float2 r0 = rk_elem<N, DIM>(ug - (unsigned)c0 * ucs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
                                       make_float2(z4.x, z4.y), Pb, pcs, kt, kd, prm, fscale, nv0, esum);
-    const float2 r1 = rk_elem<N, DIM>(g + 1 - (long long)c1 * cs, c1, make_float2(s4.z, s4.w),
+    const float2 r1 = rk_elem<N, DIM>(ug + 1u - (unsigned)c1 * ucs, c1, make_float2(s4.z, s4.w),
                                       make_float2(a4.z, a4.w), make_float2(z4.z, z4.w), Pb, pcs, kt, kd, prm,
                                       fscale, nv1, esum);
     if (prm.rk < 0) {
@@ -546,33 +623,6 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
     }
   }
   if (prm.rk == 3 && prm.want_energy) block_sum_store(esum, partial, batch * gridDim.x + blockIdx.x);
-}
-
-// ------------------------------------------------------------------------------
-// Low-wavenumber band helpers (few hundred modes; one CTA per trajectory).
-// band: 0 < |k|^2 <= kf^2 (init_fields.py:167-188). weights: half-axis multiplicity.
-// ------------------------------------------------------------------------------
-template <int DIM>
-__device__ __forceinline__ bool band_mode(int i, int N, int kf, long long& idx, int& wgt) {
-  // enumerate kx in [-kf, kf], (3D) km in [-kf, kf], kh in [0, kf]
-  const int n1 = 2 * kf + 1, nh = kf + 1;
-  const int kh = i % nh;
-  const int r = i / nh;
-  const int km = DIM == 3 ? (r % n1) - kf : 0;
-  const int kx = DIM == 3 ? (r / n1) - kf : r - kf;
-  const int k2 = kx * kx + km * km + kh * kh;
-  if (k2 == 0 || k2 > kf * kf) return false;
-  const int H = N / 2 + 1;
-  const int xi = kx < 0 ? kx + N : kx;
-  const int mi = km < 0 ? km + N : km;
-  idx = DIM == 3 ? ((long long)xi * N + mi) * H + kh : (long long)xi * H + kh;
-  wgt = (kh == 0 || kh == N / 2) ? 1 : 2;
-  return true;
-}
-
-template <int DIM>
-__device__ __forceinline__ int band_count(int kf) {
-  return DIM == 3 ? (2 * kf + 1) * (2 * kf + 1) * (kf + 1) : (2 * kf + 1) * (kf + 1);
 }
 
 // Lamorgese et al. KE rescaling (spectral_solver.py:82-112), one CTA per trajectory.
@@ -637,37 +687,6 @@ k_force_ekin(float2* __restrict__ uh, long long cs, const double* __restrict__ p
       float2 v = ub[c * cs + idx];
       ub[c * cs + idx] = make_float2(v.x * alpha, v.y * alpha);
     }
-  }
-}
-
-// Constant-power band forcing coefficient eps / (2 E_f + tiny) of the current stage
-// field (extension), one CTA per trajectory.
-template <int DIM>
-__global__ void __launch_bounds__(256)
-k_band_scale(const float2* __restrict__ uh, long long cs, int N, int kf, double inv_n2d,
-             double eps_inj, double tiny, double* __restrict__ out) {
-  const int batch = blockIdx.x;
-  const float2* ub = uh + (long long)batch * 3 * cs;
-  __shared__ double red[32];
-  double lo = 0.0;
-  const int nb = band_count<DIM>(kf);
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    long long idx;
-    int wg;
-    if (!band_mode<DIM>(i, N, kf, idx, wg)) continue;
-    for (int c = 0; c < 3; ++c) {
-      const float2 v = ub[c * cs + idx];
-      lo += wg * ((double)v.x * v.x + (double)v.y * v.y);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) lo += __shfl_xor_sync(0xffffffffu, lo, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (lane == 0) red[wid] = lo;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double L = 0.0;
-    for (int i = 0; i < nw; ++i) L += red[i];
-    out[batch] = eps_inj / (2.0 * (0.5 * L * inv_n2d) + tiny);
   }
 }
 

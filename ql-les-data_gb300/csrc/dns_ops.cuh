@@ -10,8 +10,10 @@ namespace l3es {
 template <int N>
 struct DnsOps {
   static constexpr int H = N / 2 + 1;
-  static constexpr int TX = TW * Fft<N>::T;  // threads of the strided passes
+  static constexpr int TX = TW * Fft<N>::T;  // threads of the strided x passes
   using L = LineCfg<N>;
+  using KY = KyCfg<N>;
+  static constexpr unsigned ky_tiles(int ncols) { return (unsigned)((ncols + KY::TWY - 1) / KY::TWY); }
 
   static unsigned line_blocks(long long lines) { return (unsigned)((lines + L::LPC - 1) / L::LPC); }
 
@@ -32,26 +34,24 @@ struct DnsOps {
                     us, c.cs, c.W, c.fs, c.tw));
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
-                  ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 6 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
                                                                                          c.tw));
     L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
                 line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                     c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_FWD, Adu * (1.0 + rows), s,
-                  ky_pass<N, kFwd><<<dim3(c.kt / TW, N, 3 * c.batch), TX, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd,
+                  ky_pass<N, kFwd><<<dim3(ky_tiles(c.kt), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd,
                                                                                   c.tw));
-    if (prm.band_kf2 > 0) {
-      const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
-      L3ES_LAUNCH(c, KK_BAND, 0.0, s,
-                  k_band_scale<DIM><<<c.batch, 256, 0, s>>>(us, c.cs, N, c.kf, inv_n2d, c.eps_inj, 1e-30, c.band));
-    }
     // band x-FFT + projection into P, then the elementwise RK update
     const int nb = 2 * c.kd + 1;
     const double Ap = 8.0 * 3.0 * c.pcs * B;
+    // (block 0 of each trajectory also computes the constant-power coefficient of us)
+    const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
     L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
                 kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
-                    c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw));
+                    c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
+                    c.eps_inj, c.band));
     const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 3.0 : rk < 3 ? 5.0 : 3.0);
     const long long pairs = 3 * c.cs / 2;
     L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
@@ -78,7 +78,7 @@ struct DnsOps {
                     uh, c.cs, c.W, c.fs, c.tw));
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
-                  ky_pass<N, kInv><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
                                                                                          c.tw));
     L3ES_LAUNCH(c, KK_LINE_C2R, A + P, s,
                 line_c2r<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
@@ -102,7 +102,7 @@ struct DnsOps {
                     u, c.ps, c.W, c.fs, c.tw, (int)lines));
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_FWD, 2.0 * A, s,
-                  ky_pass<N, kFwd><<<dim3((H + TW - 1) / TW, N, 3 * c.batch), TX, 0, s>>>(c.W, c.fs, H, H, N / 2,
+                  ky_pass<N, kFwd><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
                                                                                          c.tw));
     L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 2.0 * A, s,
                 kx_fwd_plain<N, DIM><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(

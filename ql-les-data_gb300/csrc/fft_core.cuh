@@ -137,10 +137,13 @@ struct Sched {
 // Exchange index per layout, chosen with a shared-memory bank model (8-byte
 // accesses served per half warp) of every Stockham read/write pattern:
 //  - column-interleaved buffers (SS > 1): one spare slot every 8 elements;
-//  - contiguous per-line buffers (SS == 1): XOR swizzle of the low 4 bits by bits
-//    3..6 (a permutation inside aligned blocks of 16), lines M + 8 slots apart.
-template <int SS>
-__device__ __forceinline__ int xpad(int n) { return SS == 1 ? n ^ ((n >> 3) & 15) : n + (n >> 3); }
+//  - contiguous per-line buffers (SS == 1): XOR swizzle of the low 4 bits (a
+//    permutation inside aligned blocks of 16) by bits 3..6 when a thread holds 8
+//    elements, by bits 4..7 when it holds 16; lines M + 8 slots apart.
+template <int SS, int E = 8>
+__device__ __forceinline__ int xpad(int n) {
+  return SS == 1 ? (E == 16 ? n ^ ((n >> 4) & 15) : n ^ ((n >> 3) & 15)) : n + (n >> 3);
+}
 template <int SS>
 __host__ __device__ constexpr int xpad_len(int n) { return SS == 1 ? n + 8 : n + n / 8; }
 
@@ -166,7 +169,7 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
     const int j = t + T * b;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      x[b][r] = FIRST ? v[b + r * BPT] : sm[xpad<SS>(j + r * (N / R)) * SS];
+      x[b][r] = FIRST ? v[b + r * BPT] : sm[xpad<SS, E>(j + r * (N / R)) * SS];
     }
   }
   if (!FIRST && !LAST) fft_sync<WARP>();  // all reads done before the in-place writes
@@ -185,7 +188,7 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
     } else {
       const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[xpad<SS>(base + r * NS) * SS] = x[b][r];
+      for (int r = 0; r < R; ++r) sm[xpad<SS, E>(base + r * NS) * SS] = x[b][r];
     }
   }
   if (!LAST) fft_sync<WARP>();
@@ -219,10 +222,18 @@ __device__ __forceinline__ void block_fft(float2 (&v)[E], float2* sm, int t,
   Stages<N, E, DIR, SS, WARP, 0>::run(v, sm, t, tw, tws);
 }
 
-// Elements per thread used for an N-point FFT.
+// Elements per thread used for an N-point FFT (radix-8 stages).
 template <int N>
 struct Fft {
   static constexpr int E = N >= 8 ? 8 : N;
+  static constexpr int T = N / E;
+};
+
+// Radix-16 variant: one exchange for N = 256 (16 x 16), half the shared-memory
+// traffic of the radix-8 schedule; used where registers allow 16 values per thread.
+template <int N>
+struct Fft16 {
+  static constexpr int E = N >= 16 ? 16 : N;
   static constexpr int T = N / E;
 };
 

@@ -315,15 +315,16 @@ static void ip_free(l3es_interp_plan* p) {
 // strided c2c passes of the NUFFT grid (inverse), via the ky_pass kernel
 template <int NG>
 static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
-  constexpr int TX = TW * Fft<NG>::T;
+  using KY = KyCfg<NG>;
+  constexpr int TX = KY::THREADS, TWY = KY::TWY;
   const long long per = p->gcs;
   if (p->dim == 3) {
     // x: pencils of stride n^2, columns = (y, z) flattened
-    ky_pass<NG, kInv><<<dim3((NG * NG + TW - 1) / TW, 1, 3), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG * NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
     // y: pencils of stride n inside each x-plane, columns = z
-    ky_pass<NG, kInv><<<dim3((NG + TW - 1) / TW, NG, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, NG, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
   } else {
-    ky_pass<NG, kInv><<<dim3((NG + TW - 1) / TW, 1, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
   }
   const long long lines = 3 * per / NG;
   constexpr int LPC = (32 / Fft<NG>::T) * 4;
