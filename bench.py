@@ -114,6 +114,19 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def replica_throughput(ms_local, world, dist=None, device="cpu"):
+    """Replicas (one independent trajectory per rank): the job time is the slowest
+    rank's, throughput = world / job time. Returns (max ms per step, steps/s)."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    return ms, world * 1e3 / ms
+
+
 def initial_field(n):
     """Host FP64 initial field of the workload (product init, l3es.init_fields)."""
     from l3es import init_fields as F
@@ -306,11 +319,7 @@ def run_ours(args):
         barrier()
     ms = e0.elapsed_time(e1) / args.steps
     clocks = clk.summary()
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
-    value = world * 1e3 / ms
+    ms, value = replica_throughput(ms, world, dist, device="cuda")
 
     # instrumented pass: per-kernel CUDA events for the roofline numerator/denominator
     plan.timing(True)
@@ -416,6 +425,155 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------
+# 24 mixed trajectories: 16 2D Kolmogorov runs (8 at 128^2, 6 at 256^2, 2 at 512^2,
+# nu in [5e-4, 2e-3], 32^2 particles each) and 8 3D HIT runs (6 at 64^3, 2 at 128^3,
+# Rogallo k4exp kp=4), seeds 0-23. Batched: one plan per size with per-trajectory
+# viscosity, the whole step (DNS + particles) recorded as one CUDA graph. Sequential:
+# one plan per trajectory, launched one after another.
+# ---------------------------------------------------------------------------------
+BATCH_GROUPS = [(2, 128, 8), (2, 256, 6), (2, 512, 2), (3, 64, 6), (3, 128, 2)]
+
+
+def _batch_runs():
+    from l3es import init_fields as F
+
+    runs, seed = [], 0
+    nus2d = np.linspace(5e-4, 2e-3, 16)
+    i2 = 0
+    for dim, n, count in BATCH_GROUPS:
+        for _ in range(count):
+            if dim == 2:
+                u = F.init_u_random2d(n, seed)
+                nu = float(nus2d[i2])
+                i2 += 1
+                dt = 1e-3
+            else:
+                u = F.init_u_hit(n, seed, spectrum="k4exp", kp=4.0)
+                u *= np.sqrt(0.5 / (0.5 * np.mean(np.sum(u * u, axis=0))))
+                nu = 5e-3
+                dx = 2 * np.pi / n
+                dt = float(CFL / (np.abs(u).max(axis=(1, 2, 3)) / dx + nu / dx**2).min())
+            runs.append(dict(dim=dim, n=n, nu=nu, dt=dt, u=u, seed=seed))
+            seed += 1
+    return runs
+
+
+def run_batch24(args):
+    import torch
+
+    from l3es import _native
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    runs = _batch_runs()
+    points = sum(r["n"] ** r["dim"] for r in runs)
+    kw2 = dict(kolm_k=4, kolm_amp=1.0, drag=0.1)
+
+    def spec(plan, u, dim, n):
+        uh = torch.empty((3, n, n, n // 2 + 1) if dim == 3 else (3, n, n // 2 + 1), dtype=torch.complex64,
+                         device="cuda")
+        tmp = _native.Plan(dim=dim, n=n, nu=0.0, dt=1.0)
+        tmp.rfftn(torch.from_numpy(u.astype(np.float32)).cuda(), uh)
+        return uh
+
+    def particles2d(seed):
+        rng = np.random.default_rng(100 + seed)
+        ax = (np.arange(32) + 0.5) * 2 * np.pi / 32
+        gx, gy = np.meshgrid(ax, ax, indexing="ij")
+        r = np.stack([gx.ravel(), gy.ravel()], 1) + rng.uniform(-0.25, 0.25, (1024, 2)) * 2 * np.pi / 32
+        return torch.from_numpy(np.mod(r, 2 * np.pi)).cuda()
+
+    # batched: one plan per size, one graph per step
+    groups, pos = [], 0
+    for dim, n, count in BATCH_GROUPS:
+        rs = runs[pos : pos + count]
+        pos += count
+        dt = min(r["dt"] for r in rs)
+        pl = _native.Plan(dim=dim, n=n, nu=0.0, dt=dt, batch=count, **(kw2 if dim == 2 else {}))
+        pl.set_nu([r["nu"] for r in rs])
+        uh = torch.stack([spec(pl, r["u"], dim, n) for r in rs]).contiguous()
+        parts = []
+        if dim == 2:
+            for b, r in enumerate(rs):
+                ip = _native.InterpPlan(dim=2, ckp_n=32, n_fine=n, np_max=1024)
+                rr = [particles2d(r["seed"]), torch.empty(1024, 2, dtype=torch.float64, device="cuda")]
+                parts.append((ip, b, rr, torch.empty(1024, 2, dtype=torch.float64, device="cuda"), dt))
+        groups.append((pl, uh, parts))
+
+    def record(graph_pingpong):
+        cap = _native.Graph.begin()
+        for pl, uh, parts in groups:
+            pl.step(uh, 1, stream=cap)
+            for ip, b, rr, ur, dt in parts:
+                ip.set_spectrum(uh[b], stream=cap)
+                src, dst = (rr[0], rr[1]) if graph_pingpong == 0 else (rr[1], rr[0])
+                ip.interp(src, ur, dt=dt, r_out=dst, stream=cap)
+        return _native.Graph.end(cap)
+
+    graphs = [record(0), record(1)]
+    steps = args.batch_steps
+    for i in range(args.warmup):
+        graphs[i % 2].launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        e0.record()
+        for i in range(steps):
+            graphs[i % 2].launch()
+        e1.record()
+        torch.cuda.synchronize()
+    t_batched = e0.elapsed_time(e1) / 1e3
+    batched_rate = points * steps / t_batched
+
+    # sequential per-run launches (no batching, no graph)
+    singles = []
+    for r in runs:
+        pl = _native.Plan(dim=r["dim"], n=r["n"], nu=r["nu"], dt=r["dt"], **(kw2 if r["dim"] == 2 else {}))
+        uh = spec(pl, r["u"], r["dim"], r["n"])
+        part = None
+        if r["dim"] == 2:
+            ip = _native.InterpPlan(dim=2, ckp_n=32, n_fine=r["n"], np_max=1024)
+            part = (ip, [particles2d(r["seed"]), torch.empty(1024, 2, dtype=torch.float64, device="cuda")],
+                    torch.empty(1024, 2, dtype=torch.float64, device="cuda"))
+        singles.append((pl, uh, part, r["dt"]))
+    seq_steps = max(10, steps // 5)
+
+    def seq_step():
+        for pl, uh, part, dt in singles:
+            pl.step(uh, 1)
+            if part is not None:
+                ip, rr, ur = part
+                ip.set_spectrum(uh)
+                ip.interp(rr[0], ur, dt=dt, r_out=rr[1])
+                rr.reverse()
+
+    for _ in range(args.warmup):
+        seq_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(seq_steps):
+        seq_step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_seq = e0.elapsed_time(e1) / 1e3
+    seq_rate = points * seq_steps / t_seq
+    line = {
+        "metric": "grid-point updates/s, 24 mixed 2D/3D trajectories (DNS + particles)", "value": batched_rate,
+        "unit": "grid-point updates/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_batched / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (fp64 reductions)", "data": "synthetic",
+        "config": {"workload": "batch24: 2D Kolmogorov 8x128^2 + 6x256^2 + 2x512^2 (32^2 particles each), "
+                               "3D HIT 6x64^3 + 2x128^3", "grid_points_per_step": points,
+                   "batched": "5 plans (one per size, per-trajectory nu) + 16 particle plans, one CUDA graph per step"},
+        "sequential": {"value": seq_rate, "steps": seq_steps, "ms_per_step": 1e3 * t_seq / seq_steps,
+                       "note": "24 single-trajectory plans launched one after another"},
+        "speedup_vs_sequential": batched_rate / seq_rate,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,6 +581,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--workload", default="hit256", choices=["hit256", "batch24"],
+                    help="hit256: the metric's 256^3 step; batch24: 24 mixed trajectories")
+    ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--ke-steps", type=int, default=200,
                     help="steps of the FP32-vs-FP64 kinetic energy check (0 = skip)")
     ap.add_argument("--skip-baselines", action="store_true",
@@ -430,7 +591,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    return run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_batch24(args) if args.workload == "batch24" else run_ours(args)
 
 
 if __name__ == "__main__":

@@ -69,6 +69,10 @@ int l3es_plan_destroy(l3es_plan* plan);
  * the reference computes it once in set_up_solver (spectral_solver.py:209). */
 int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count);
 
+/* Per-trajectory viscosities (host array of `batch` doubles); the plan starts with
+ * desc->nu for every trajectory. */
+int l3es_plan_set_nu(l3es_plan* plan, const double* nu_host, int32_t count);
+
 /* Scratch bytes the plan holds on the device (for capacity planning). */
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
 
@@ -178,6 +182,20 @@ int l3es_interp_dft_noalloc(int32_t dim, int32_t n_fine, int32_t ckp_n, const vo
  * (l3es/integrator.py:21-23). */
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,
                double* out, void* stream);
+
+/* ---- CUDA graphs: record library calls once, replay them as one launch ----
+ * No counterpart in the reference (its step is one XLA executable per trajectory,
+ * spectral_solver.py:130-153). l3es_graph_begin returns a capturing stream; l3es_step,
+ * l3es_rhs, l3es_interp*, l3es_shift and the diagnostics called with that stream are
+ * recorded, not run (plan creation, l3es_plan_set_*, kernel timing and
+ * l3es_interp_dft_noalloc's first call must happen before); l3es_graph_end turns the
+ * recording into a graph that l3es_graph_launch runs on any stream, with the device
+ * pointers it was recorded with. */
+typedef struct l3es_graph l3es_graph;
+int l3es_graph_begin(void** capture_stream);
+int l3es_graph_end(void* capture_stream, l3es_graph** out);
+int l3es_graph_launch(l3es_graph* graph, void* stream);
+int l3es_graph_destroy(l3es_graph* graph);
 
 /* Last error message of the calling thread ("" if none). */
 const char* l3es_last_error(void);

@@ -547,6 +547,7 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
   const int km = DIM == 3 ? kfull(mid, N) : 0;
   const int ik2 = kx * kx + km * km + kh * kh;
   const float kk2 = (float)ik2;
+  const float nu = prm.nu;
   float2 r = make_float2(0.f, 0.f);
   // band rows as unsigned offsets: in the band iff 0 <= k + kd <= 2 kd on every axis
   const unsigned nb = 2u * (unsigned)kd + 1u;
@@ -556,8 +557,8 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
     const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
     r = __ldg(P + c * pcs + row * kt + kh);
   }
-  r.x -= prm.nu * kk2 * sv.x;
-  r.y -= prm.nu * kk2 * sv.y;
+  r.x -= nu * kk2 * sv.x;
+  r.y -= nu * kk2 * sv.y;
   if (prm.drag != 0.f) {
     r.x -= prm.drag * sv.x;
     r.y -= prm.drag * sv.y;
@@ -591,8 +592,9 @@ template <int N, int DIM>
 __global__ void __launch_bounds__(256)
 k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const float2* us, const float2* u0,
             float2* acc, float2* out, float2* fin, long long cs, EpiParams prm,
-            const double* __restrict__ band_scale, double* __restrict__ partial) {
+            const double* __restrict__ band_scale, double* __restrict__ partial, const float* __restrict__ nu_b) {
   const int batch = blockIdx.y;
+  prm.nu = nu_b[batch];  // per-trajectory viscosity
   const long long pairs = 3 * cs / 2;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long bo = (long long)batch * 3 * cs;

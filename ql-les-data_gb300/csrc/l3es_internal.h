@@ -128,6 +128,7 @@ struct Ctx {
   double* band = nullptr;      // [batch] constant-power coefficient
   double* e0 = nullptr;        // [batch] ekin_tot targets
   double* einj = nullptr;      // [batch] scratch e_inj
+  float* nu_b = nullptr;       // [batch] viscosity per trajectory
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate
   KTimer* timer = nullptr;     // per-launch timing (nullptr = off)

@@ -200,6 +200,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.band, sizeof(double) * B, "band");
   rc = rc ? rc : plan_alloc(p, (void**)&c.e0, sizeof(double) * B, "e0");
   rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.nu_b, sizeof(float) * B, "viscosities");
   if (rc != L3ES_OK) {
     plan_free(p);
     delete p;
@@ -207,7 +208,9 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   }
   std::vector<float2> tw = twiddles(n);
   std::vector<double> e0(B, desc->e_kin_init);
+  std::vector<float> nus(B, (float)desc->nu);
   cudaError_t e = cudaMemcpy(c.tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c.nu_b, nus.data(), sizeof(float) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -233,6 +236,18 @@ int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count) {
   if (count != plan->ctx.batch) return fail(L3ES_EINVAL, "l3es_plan_set_e0: count != batch");
   return cuda_check(cudaMemcpy(plan->ctx.e0, e0_host, sizeof(double) * count, cudaMemcpyHostToDevice),
                     "l3es_plan_set_e0");
+}
+
+int l3es_plan_set_nu(l3es_plan* plan, const double* nu_host, int32_t count) {
+  if (!plan || !nu_host) return fail(L3ES_EINVAL, "l3es_plan_set_nu: null argument");
+  if (count != plan->ctx.batch) return fail(L3ES_EINVAL, "l3es_plan_set_nu: count != batch");
+  std::vector<float> v(count);
+  for (int i = 0; i < count; ++i) {
+    if (!(nu_host[i] >= 0.0)) return fail(L3ES_EINVAL, "l3es_plan_set_nu: viscosity must be >= 0");
+    v[i] = (float)nu_host[i];
+  }
+  return cuda_check(cudaMemcpy(plan->ctx.nu_b, v.data(), sizeof(float) * count, cudaMemcpyHostToDevice),
+                    "l3es_plan_set_nu");
 }
 
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan) { return plan ? plan->ws_bytes : 0; }

@@ -25,6 +25,11 @@ _SIGNATURES = {
     "l3es_plan_destroy": (ctypes.c_int, [_P]),
     "l3es_plan_set_e0": (ctypes.c_int, [_P, _P, _I]),
     "l3es_plan_workspace_bytes": (ctypes.c_int64, [_P]),
+    "l3es_plan_set_nu": (ctypes.c_int, [_P, _P, _I]),
+    "l3es_graph_begin": (ctypes.c_int, [ctypes.POINTER(_P)]),
+    "l3es_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "l3es_graph_launch": (ctypes.c_int, [_P, _P]),
+    "l3es_graph_destroy": (ctypes.c_int, [_P]),
     "l3es_step": (ctypes.c_int, [_P, _P, _P, _I, _P, _P]),
     "l3es_rhs": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_rfftn": (ctypes.c_int, [_P, _P, _P, _P]),
@@ -167,6 +172,11 @@ class Plan:
     def set_e0(self, e0) -> None:
         vals = (ctypes.c_double * self.batch)(*[float(v) for v in (e0 if hasattr(e0, "__len__") else [e0] * self.batch)])
         _check(self._lib.l3es_plan_set_e0(self._h, vals, self.batch), "l3es_plan_set_e0")
+
+    def set_nu(self, nu) -> None:
+        """Per-trajectory viscosities (one value per batch member)."""
+        vals = (ctypes.c_double * self.batch)(*[float(v) for v in (nu if hasattr(nu, "__len__") else [nu] * self.batch)])
+        _check(self._lib.l3es_plan_set_nu(self._h, vals, self.batch), "l3es_plan_set_nu")
 
     def step(self, u_hat, nsteps: int = 1, u_out=None, e_inj=None, stream=None) -> None:
         """In-place RK4 steps on u_hat (optionally irfftn into u_out at the end)."""
@@ -335,3 +345,50 @@ def interp_dft_noalloc(dim: int, n_fine: int, ckp_n: int, u_hat_fine, r, u_r, st
         raise ValueError("positions and velocities are float64 (np, dim)")
     _check(load().l3es_interp_dft_noalloc(int(dim), int(n_fine), int(ckp_n), _ptr(u_hat_fine), _ptr(r),
                                           int(r.shape[0]), _ptr(u_r), _stream(stream)), "l3es_interp_dft_noalloc")
+
+
+class _CaptureStream:
+    """A capturing stream handle, accepted wherever a ``stream=`` argument is."""
+
+    def __init__(self, handle: int):
+        self.cuda_stream = handle
+
+
+class Graph:
+    """Library calls recorded once and replayed as one CUDA graph launch.
+
+        cap = Graph.begin()
+        plan_a.step(uh_a, 1, stream=cap); plan_b.step(uh_b, 1, stream=cap)
+        g = Graph.end(cap)
+        for _ in range(steps): g.launch()
+    """
+
+    def __init__(self, handle):
+        self._h = handle
+        self._lib = load()
+
+    @staticmethod
+    def begin() -> _CaptureStream:
+        h = ctypes.c_void_p()
+        _check(load().l3es_graph_begin(ctypes.byref(h)), "l3es_graph_begin")
+        return _CaptureStream(h.value)
+
+    @staticmethod
+    def end(cap: _CaptureStream) -> "Graph":
+        h = ctypes.c_void_p()
+        _check(load().l3es_graph_end(cap.cuda_stream, ctypes.byref(h)), "l3es_graph_end")
+        return Graph(h)
+
+    def launch(self, stream=None) -> None:
+        _check(self._lib.l3es_graph_launch(self._h, _stream(stream)), "l3es_graph_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.l3es_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,144 @@
+"""Batched trajectories and CUDA-graph replay on the GPU.
+
+A plan with batch > 1 steps several same-size trajectories in one launch per kernel
+(per-trajectory viscosity and ekin_tot target); it must give each trajectory the
+result of its own single plan. A graph recorded from library calls must replay to
+the same bits as the calls run directly.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import numpy_ref as R
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _fields(dim, n, count, seed):
+    out = []
+    for b in range(count):
+        if dim == 3:
+            u = R.init_u_hit(n, seed + b, "k4exp", 3.0)
+            u *= np.sqrt(0.5 / R.kinetic_energy(u))
+        else:
+            u = R.init_u_random2d(n, seed + b)
+        out.append(u)
+    return out
+
+
+def _spec(plan_cls, dim, n, u):
+    p = plan_cls(dim=dim, n=n, nu=0.01, dt=1e-3)
+    uh = torch.empty(p.spec_shape, dtype=torch.complex64, device="cuda")
+    p.rfftn(torch.from_numpy(np.ascontiguousarray(u, dtype=np.float32)).cuda(), uh)
+    return uh
+
+
+@pytest.mark.parametrize("dim,n,forcing", [(3, 32, "ekin_tot"), (3, 32, "const_power"), (2, 64, "none")])
+def test_batched_plan_matches_single_plans(dim, n, forcing):
+    from l3es import _native
+
+    count, dt, steps = 3, 2e-3, 3
+    nus = [4e-3, 8e-3, 1.2e-2]
+    us = _fields(dim, n, count, 11)
+    e0s = [R.kinetic_energy(u) for u in us]
+    kw = dict(forcing=forcing, kf=2 if forcing != "none" else 0, eps_inj=0.1)
+    singles = []
+    for b in range(count):
+        p = _native.Plan(dim=dim, n=n, nu=nus[b], dt=dt, e_kin_init=e0s[b], **kw)
+        uh = _spec(_native.Plan, dim, n, us[b])
+        p.step(uh, steps)
+        singles.append(uh.cpu().numpy())
+    pb = _native.Plan(dim=dim, n=n, nu=0.0, dt=dt, batch=count, **kw)
+    pb.set_nu(nus)
+    pb.set_e0(e0s)
+    uhb = torch.stack([_spec(_native.Plan, dim, n, u) for u in us]).contiguous()
+    einj = torch.zeros(steps * count, dtype=torch.float64, device="cuda")
+    pb.step(uhb, steps, e_inj=einj)
+    got = uhb.cpu().numpy()
+    for b in range(count):
+        assert np.array_equal(got[b], singles[b]) or \
+            np.abs(got[b] - singles[b]).max() <= 1e-6 * np.abs(singles[b]).max()
+    if forcing == "ekin_tot":
+        ke = torch.zeros(count, dtype=torch.float64, device="cuda")
+        pb.kinetic_energy(uhb, ke)
+        np.testing.assert_allclose(ke.cpu().numpy(), e0s, rtol=1e-6)
+
+
+def test_graph_replay_equals_direct_calls():
+    from l3es import _native
+
+    n, steps = 32, 5
+    u = _fields(3, n, 1, 5)[0]
+    p = _native.Plan(dim=3, n=n, nu=5e-3, dt=2e-3, forcing="const_power", kf=2, eps_inj=0.1)
+    ip = _native.InterpPlan(dim=3, ckp_n=16, n_fine=n, np_max=500)
+    rng = np.random.default_rng(0)
+    r0 = torch.from_numpy(rng.uniform(0, 2 * np.pi, (500, 3))).cuda()
+
+    # direct
+    uh_d = _spec(_native.Plan, 3, n, u)
+    r_d = [r0.clone(), torch.empty_like(r0)]
+    ur_d = torch.empty_like(r0)
+    for _ in range(steps):
+        p.step(uh_d, 1)
+        ip.set_spectrum(uh_d)
+        ip.interp(r_d[0], ur_d, dt=2e-3, r_out=r_d[1])
+        r_d.reverse()
+    # recorded once (two steps with the ping-pong positions), replayed
+    uh_g = _spec(_native.Plan, 3, n, u)
+    r_a, r_b = r0.clone(), torch.empty_like(r0)
+    ur_g = torch.empty_like(r0)
+    cap = _native.Graph.begin()
+    for src, dst in ((r_a, r_b), (r_b, r_a)):
+        p.step(uh_g, 1, stream=cap)
+        ip.set_spectrum(uh_g, stream=cap)
+        ip.interp(src, ur_g, dt=2e-3, r_out=dst, stream=cap)
+    g = _native.Graph.end(cap)
+    for _ in range(steps // 2):
+        g.launch()
+    # one more step directly to reach 5
+    p.step(uh_g, 1)
+    ip.set_spectrum(uh_g)
+    ip.interp(r_a, ur_g, dt=2e-3, r_out=r_b)
+    torch.cuda.synchronize()
+    assert torch.equal(uh_g, uh_d)
+    assert torch.equal(ur_g, ur_d)
+    assert torch.equal(r_b, r_d[0])
+
+
+def test_graph_of_two_grid_sizes():
+    from l3es import _native
+
+    pa = _native.Plan(dim=2, n=64, nu=1e-3, dt=1e-3, kolm_k=4, kolm_amp=1.0, drag=0.1)
+    pb = _native.Plan(dim=3, n=32, nu=5e-3, dt=2e-3)
+    ua, ub = _fields(2, 64, 1, 1)[0], _fields(3, 32, 1, 2)[0]
+    ref_a, ref_b = _spec(_native.Plan, 2, 64, ua), _spec(_native.Plan, 3, 32, ub)
+    pa.step(ref_a, 4)
+    pb.step(ref_b, 4)
+    ga, gb = _spec(_native.Plan, 2, 64, ua), _spec(_native.Plan, 3, 32, ub)
+    cap = _native.Graph.begin()
+    pa.step(ga, 1, stream=cap)
+    pb.step(gb, 1, stream=cap)
+    g = _native.Graph.end(cap)
+    for _ in range(4):
+        g.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(ga, ref_a) and torch.equal(gb, ref_b)
+
+
+def test_kolmogorov_drag_extension_matches_oracle():
+    """2D extension terms (f_x = sin(4y), drag 0.1) vs the oracle's opt-in terms."""
+    from l3es import _native
+
+    n, nu, dt, steps = 64, 1e-3, 1e-3, 3
+    u = _fields(2, n, 1, 7)[0]
+    uh0 = np.fft.rfftn(u, axes=(1, 2)).squeeze()
+    rhs = R.rhs_wrapper(n, nu, (1, 2), drag=0.1, force_hat=R.kolmogorov_forcing_hat(n, 1.0, 4))
+    step = R.rk4_wrapper(dt, rhs, None, 0.0, "none", (1, 2))
+    uu, uh = u, uh0
+    for _ in range(steps):
+        uu, uh, _ = step(uu, uh)
+    p = _native.Plan(dim=2, n=n, nu=nu, dt=dt, kolm_k=4, kolm_amp=1.0, drag=0.1)
+    g = torch.from_numpy(np.ascontiguousarray(uh0, dtype=np.complex64)).cuda()
+    p.step(g, steps)
+    assert np.abs(g.cpu().numpy() - uh).max() < 2e-5 * np.abs(uh).max()
