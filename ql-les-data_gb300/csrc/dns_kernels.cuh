@@ -206,6 +206,30 @@ __device__ __forceinline__ float2 r2c_unpack(const float2* Z, int k, int M,
   return make_float2(0.5f * (s.x + id.x), 0.5f * (s.y + id.y));
 }
 
+// r2c outputs X[k], k = t + T e, from an M-point forward FFT held in registers
+// (v[e] = Z[t + T e]); the partner Z[M - k] comes from lane (T - t) mod T by shuffle
+// (slot E-1-e, or (E-e) mod E for t = 0, whose e = 0 partner is Z[M] = Z[0]).
+template <int M, int E>
+__device__ __forceinline__ void r2c_unpack_regs(const float2 (&v)[E], int t, const float2* __restrict__ twN,
+                                                float2 (&X)[E]) {
+  constexpr int T = M / E;
+  const int lane = threadIdx.x & 31;
+  const int src = lane - t + (t == 0 ? 0 : T - t);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const float2 give = (t == 0) ? v[(E - e) % E] : v[E - 1 - e];
+    float2 zm;
+    zm.x = __shfl_sync(0xffffffffu, give.x, src);
+    zm.y = __shfl_sync(0xffffffffu, give.y, src);
+    const float2 zk = v[e];
+    const int k = t + T * e;
+    const float2 s = make_float2(zk.x + zm.x, zk.y - zm.y);
+    const float2 d = make_float2(zk.x - zm.x, zk.y + zm.y);
+    const float2 id = mul_i<kFwd>(cmul(__ldg(twN + k), d));  // -i W^k d
+    X[e] = make_float2(0.5f * (s.x + id.x), 0.5f * (s.y + id.y));
+  }
+}
+
 // ------------------------------------------------------------------------------
 // Half-axis line pass of the RHS: 6 half-spectrum lines (u, curl u) -> c2r -> u x
 // curl u -> r2c of the 3 products, written for k <= kd (zeros up to kt). scale
@@ -238,7 +262,7 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   for (int f = 0; f < 6; ++f) {
     float2 v[E];
     c2r_load_pack<M, E>(src + f * fs, t, v, twN, scale);
-    block_fft<M, E, kInv, 1, true>(v, xs, t, twN, 2);
+    warp_fft<M, E, kInv>(v, xs, t, twN, 2);
     // v[e] packs the physical values at 2n and 2n+1, n = t + T*e
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -271,14 +295,17 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   float2* db = du + (long long)batch * 3 * ds + line * kt;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    block_fft<M, E, kFwd, 1, true>(cr[c], xs, t, twN, 2);
-    __syncwarp();
-#pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad<1, E>(t + T * e)] = cr[c][e];
-    __syncwarp();
+    warp_fft<M, E, kFwd>(cr[c], xs, t, twN, 2);
+    float2 X[E];
+    r2c_unpack_regs<M, E>(cr[c], t, twN, X);
     if (valid) {
       float2* dst = db + c * ds;
-      for (int k = t; k < kt; k += T) dst[k] = k <= kd ? r2c_unpack<E>(xs, k, M, twN) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int k = t + T * e;
+        if (k < kt) dst[k] = k <= kd ? X[e] : make_float2(0.f, 0.f);
+      }
+      for (int k = M + t; k < kt; k += T) dst[k] = make_float2(0.f, 0.f);  // kt > M only for tiny N
     }
     __syncwarp();
   }
@@ -305,7 +332,7 @@ line_c2r(const float2* __restrict__ w, long long fs, float* __restrict__ out, lo
     const float2* src = w + (long long)batch * 3 * fs + f * fs + line * H;
     float2 v[E];
     c2r_load_pack<M, E>(src, t, v, twN, scale);
-    block_fft<M, E, kInv, 1, true>(v, xs, t, twN, 2);
+    warp_fft<M, E, kInv>(v, xs, t, twN, 2);
     if (valid) {
       float2* dst = reinterpret_cast<float2*>(out + (long long)batch * 3 * os + f * os + line * N);
 #pragma unroll
@@ -337,14 +364,14 @@ line_r2c(const float* __restrict__ in, long long is, float2* __restrict__ w, lon
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = __ldg(src + t + T * e);
-    block_fft<M, E, kFwd, 1, true>(v, xs, t, twN, 2);
-    __syncwarp();
-#pragma unroll
-    for (int e = 0; e < E; ++e) xs[xpad<1, E>(t + T * e)] = v[e];
-    __syncwarp();
+    warp_fft<M, E, kFwd>(v, xs, t, twN, 2);
+    float2 X[E];
+    r2c_unpack_regs<M, E>(v, t, twN, X);
     if (valid) {
       float2* dst = w + (long long)batch * 3 * fs + f * fs + line * H;
-      for (int k = t; k < H; k += T) dst[k] = r2c_unpack<E>(xs, k, M, twN);
+#pragma unroll
+      for (int e = 0; e < E; ++e) dst[t + T * e] = X[e];
+      if (t == 0) dst[M] = make_float2(v[0].x - v[0].y, 0.f);  // X[M] = Re Z0 - Im Z0
     }
     __syncwarp();
   }

@@ -222,6 +222,60 @@ __device__ __forceinline__ void block_fft(float2 (&v)[E], float2* sm, int t,
   Stages<N, E, DIR, SS, WARP, 0>::run(v, sm, t, tw, tws);
 }
 
+// N-point FFT whose T = N/E threads sit in one warp (per-line buffers, SS = 1). For
+// N = 2 E^2 (e.g. 128 = 8 x 8 x 2) the final radix-2 stage pairs element j with
+// j + N/2; after the second stage they sit in the same register slot of lanes t and
+// t ^ E, so that stage exchanges by warp shuffle instead of a shared-memory round
+// trip. Other sizes use the shared-memory Stockham schedule.
+template <int N, int E, int DIR>
+__device__ __forceinline__ void warp_fft(float2 (&v)[E], float2* sm, int t, const float2* __restrict__ tw,
+                                         int tws) {
+  using Sc = Sched<N, E>;
+  constexpr bool kTail2 = Sc::kStages == 3 && Sc::radix(0) == E && Sc::radix(1) == E && Sc::radix(2) == 2 &&
+                          N / E == 2 * E && N / E <= 32;
+  if constexpr (!kTail2) {
+    block_fft<N, E, DIR, 1, true>(v, sm, t, tw, tws);
+  } else {
+    constexpr int T = N / E;
+    // stage 0: radix E on the registers, out to shared memory
+    stockham_stage<N, E, E, 1, DIR, 1, true, true, false>(v, sm, t, tw, tws);
+    // stage 1: radix E (Ns = E), one butterfly per thread, outputs stay in registers:
+    // slot r holds element (t / E) N/2 + t % E + r E
+    {
+      float2 x[E];
+#pragma unroll
+      for (int r = 0; r < E; ++r) x[r] = sm[xpad<1, E>(t + r * (N / E))];
+      const int jm = t % E;
+#pragma unroll
+      for (int r = 1; r < E; ++r) x[r] = cmul(x[r], twid<DIR>(tw, r * jm * (N / (E * E)) * tws));
+      Dft<E, DIR>::run(x);
+#pragma unroll
+      for (int r = 0; r < E; ++r) v[r] = x[r];
+    }
+    // stage 2: radix 2 (Ns = N/2) between lanes t and t ^ E
+    {
+      const bool hi = t >= E;
+      const int partner = (threadIdx.x & 31) ^ E;
+      float2 y[E];
+#pragma unroll
+      for (int b = 0; b < E / 2; ++b) {
+        const float2 give = hi ? v[2 * b] : v[2 * b + 1];
+        float2 got;
+        got.x = __shfl_sync(0xffffffffu, give.x, partner);
+        got.y = __shfl_sync(0xffffffffu, give.y, partner);
+        const float2 a = hi ? got : v[2 * b];
+        float2 c = hi ? v[2 * b + 1] : got;
+        const int j = t + T * b;
+        c = cmul(c, twid<DIR>(tw, j * tws));
+        y[b] = cadd(a, c);
+        y[b + E / 2] = csub(a, c);
+      }
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = y[e];
+    }
+  }
+}
+
 // Elements per thread used for an N-point FFT (radix-8 stages).
 template <int N>
 struct Fft {
