@@ -178,6 +178,13 @@ int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r
 int l3es_interp_dft_noalloc(int32_t dim, int32_t n_fine, int32_t ckp_n, const void* u_hat_fine,
                             const double* r, int64_t np, double* u_r, void* stream);
 
+/* Particle velocities to the plan's coarse grid by the exact DFT of ur_to_u_dft_wrapper
+ * (l3es/turbulence.py:299-339): S(k) = sum_j u_r[j] exp(-i k.r_j) on the full c^dim
+ * grid, u_grid = real(ifftn(S)), float32 (3, c, c, c) / (3, c, c) (third component
+ * zero in 2D). r, u_r: float64 (np, dim). */
+int l3es_interp_particles_to_grid(l3es_interp_plan* plan, const double* r, const double* u_r,
+                                  int64_t np, float* u_grid, void* stream);
+
 /* shift_fn(r, scale * dr) = (r + scale * dr) mod box, elementwise over n doubles
  * (l3es/integrator.py:21-23). */
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,

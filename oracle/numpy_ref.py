@@ -498,3 +498,20 @@ def pos_init_cartesian(L, c, dim, jitter=0.0, seed=0):
         rng = np.random.default_rng(seed)
         r = r + rng.uniform(-jitter, jitter, size=r.shape) * dx
     return np.mod(r, L)
+
+
+# ---------------------------------------------------------------------------------
+# particle -> grid analysis (l3es/turbulence.py:299-339)
+# ---------------------------------------------------------------------------------
+def particles_to_grid_dft(r, u_r, n):
+    """ur_to_u_dft_wrapper(N, L, dim): S(k) = sum_j u_r[j] exp(-i k.r_j) for k on the
+    full n^dim grid (fftfreq order), u_grid = real(ifftn(S)); returns (dim, n, ..., n)."""
+    dim = r.shape[1]
+    k = np.fft.fftfreq(n, 1.0 / n)
+    K = np.array(np.meshgrid(*([k] * dim), indexing="ij")).reshape(dim, -1)
+    S = np.zeros((u_r.shape[1], K.shape[1]), dtype=np.complex128)
+    for s in range(0, len(r), 4096):
+        ph = np.exp(-1j * (r[s : s + 4096] @ K))  # (chunk, modes)
+        S += u_r[s : s + 4096].T @ ph
+    S = S.reshape((u_r.shape[1],) + (n,) * dim)
+    return np.real(np.fft.ifftn(S, axes=tuple(range(1, dim + 1))))

@@ -1,0 +1,98 @@
+"""FP64 NumPy restatement of the l3es SPH particle relaxation and density.
+
+TEST INFRASTRUCTURE ONLY (oracle); never on the product path.
+
+Follows l3es/relax.py:16-111 (relax_wrapper.loop_body), l3es/utils.py:169-218
+(rho_computer) and the relaxation block of the combined loop (combined.py:132-142).
+Those call jax_sph 0.1.0 (poetry.lock:832), which is neither vendored nor installed;
+its pieces are restated from their published definitions:
+  - QuinticKernel(h, dim): Morris et al. (1997) quintic spline with cutoff 3h,
+    W(q) = sigma (max(0,3-q)^5 - 6 max(0,2-q)^5 + 15 max(0,1-q)^5), q = r/h,
+    sigma = 1/(120 h), 7/(478 pi h^2), 3/(359 pi h^3) in 1, 2, 3 dimensions;
+  - TaitEoS(p_ref, rho_ref, p_background, gamma): p = p_ref ((rho/rho_ref)^gamma - 1)
+    + p_background;
+  - neighbor_list(..., mask_self=False): every pair with distance below the cutoff,
+    the particle itself included, periodic minimum-image displacements.
+PARITY UNPINNED: no reference output exists for these paths (jax_sph is absent), so
+the restatement is checked only for internal consistency (symmetry, constant density
+on a lattice, momentum conservation).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+EPS = float(np.finfo(np.float64).eps)
+
+SIGMA = {1: lambda h: 1.0 / (120.0 * h), 2: lambda h: 7.0 / (478.0 * np.pi * h * h),
+         3: lambda h: 3.0 / (359.0 * np.pi * h**3)}
+
+
+def quintic_w(r, h, dim):
+    q = r / h
+    q1, q2, q3 = (np.maximum(0.0, a - q) for a in (1.0, 2.0, 3.0))
+    return SIGMA[dim](h) * (q3**5 - 6.0 * q2**5 + 15.0 * q1**5)
+
+
+def quintic_grad_w(r, h, dim):
+    """dW/dr."""
+    q = r / h
+    q1, q2, q3 = (np.maximum(0.0, a - q) for a in (1.0, 2.0, 3.0))
+    return SIGMA[dim](h) / h * (-5.0 * q3**4 + 30.0 * q2**4 - 75.0 * q1**4)
+
+
+def _pairs(r, L, cutoff):
+    """All (i, j, r_i - r_j wrapped) with |r_i - r_j| < cutoff, self pairs included."""
+    from scipy.spatial import cKDTree
+
+    tree = cKDTree(np.mod(r, L), boxsize=L)
+    pairs = tree.query_pairs(cutoff, output_type="ndarray")
+    n = len(r)
+    i = np.concatenate([pairs[:, 0], pairs[:, 1], np.arange(n)])
+    j = np.concatenate([pairs[:, 1], pairs[:, 0], np.arange(n)])
+    d = r[i] - r[j]
+    d -= L * np.round(d / L)
+    return i, j, d
+
+
+def density(r, N, dim, L=2 * np.pi):
+    """rho_computer(N, dim, L)(r) (utils.py:169-218): mass sum_j W(|r_ij|)."""
+    dx = L / N
+    i, j, d = _pairs(r, L, 3.0 * dx)
+    dist = np.sqrt(np.sum(d * d, axis=1))
+    rho = np.zeros(len(r))
+    np.add.at(rho, i, quintic_w(dist, dx, dim))
+    return dx**dim * rho
+
+
+def relax_acceleration(r, N, dim, u_ref, L=2 * np.pi):
+    """relax_wrapper(N, dim, L, is_physical=True, u_ref).loop_body (relax.py:73-111):
+    pressure (Tait, gamma 1, c = 10 u_ref) plus the transport-velocity term."""
+    dx = L / N
+    mass = dx**dim
+    p_eos = (10.0 * u_ref) ** 2
+    i, j, d = _pairs(r, L, 3.0 * dx)
+    dist = np.sqrt(np.sum(d * d, axis=1))
+    rho = np.zeros(len(r))
+    np.add.at(rho, i, mass * quintic_w(dist, dx, dim))
+    p = p_eos * (rho - 1.0)
+    e = d / (dist[:, None] + EPS)
+    grad = quintic_grad_w(dist, dx, dim)[:, None] * e
+    ri, rj, pi, pj = rho[i], rho[j], p[i], p[j]
+    p_ij = (rj * pi + ri * pj) / (ri + rj)
+    pref = mass * ((1.0 / ri) ** 2 + (1.0 / rj) ** 2)
+    acc = (-pref * p_ij)[:, None] * grad + (0.5 * pref * (-p_eos))[:, None] * grad
+    out = np.zeros_like(r)
+    np.add.at(out, i, acc)
+    return out
+
+
+def relax_velocity(r0, u_r, dt, relax_dt_factor, N, dim, u_ref, L=2 * np.pi):
+    """combined.py:132-142: move to the next positions, one relaxation kick, and the
+    velocity that reaches the relaxed positions in one step (minimum image)."""
+    r_temp = np.mod(r0 + dt * u_r, L)
+    a = relax_acceleration(r_temp, N, dim, u_ref, L)
+    r_temp = np.mod(r_temp + (relax_dt_factor * dt) ** 2 * a, L)
+    d = r_temp - r0
+    d -= L * np.round(d / L)
+    return d / dt

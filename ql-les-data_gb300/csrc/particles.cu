@@ -81,7 +81,8 @@ k_nufft_prep(const float2* __restrict__ hh, long long hcs, int c, const float* _
 // ------------------------------------------------------------------------------
 template <int NL>
 __global__ void __launch_bounds__(128)
-line_c2c_re(const float2* __restrict__ g, float* __restrict__ gre, long long nlines, const float2* __restrict__ tw) {
+line_c2c_re(const float2* __restrict__ g, float* __restrict__ gre, long long nlines, const float2* __restrict__ tw,
+            float scale) {
   constexpr int E = Fft<NL>::E, T = Fft<NL>::T;
   static_assert(T <= 32, "line inside one warp");
   constexpr int LPC = (32 / T) * 4;
@@ -97,7 +98,7 @@ line_c2c_re(const float2* __restrict__ g, float* __restrict__ gre, long long nli
   block_fft<NL, E, kInv, 1, true>(v, s_x + q * XS, t, tw, 1);
   if (valid) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) gre[line * NL + t + T * e] = v[e].x;
+    for (int e = 0; e < E; ++e) gre[line * NL + t + T * e] = scale * v[e].x;
   }
 }
 
@@ -228,6 +229,72 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
   }
 }
 
+// ------------------------------------------------------------------------------
+// Particle -> grid spectrum (turbulence.py:299-339, ur_to_u_dft_wrapper):
+// S_c(k) = sum_j u_r[j][c] exp(-i k . r_j) for every k of the N^dim grid in fftfreq
+// order. One thread per mode; particles streamed through shared memory in tiles of
+// 128 with per-particle 1D phase tables exp(-i k_d x_d) (FP64 sincos, stored FP32);
+// tile sums in FP32, running total in FP64.
+// ------------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(128)
+k_p2g_dft(const double* __restrict__ r, const double* __restrict__ u_r, long long np, int ncomp, int n,
+          float2* __restrict__ S, long long scs) {
+  extern __shared__ float2 sh[];            // [128][DIM][n] phases
+  __shared__ float su[128][3];              // velocities of the tile
+  const long long modes = DIM == 3 ? (long long)n * n * n : (long long)n * n;
+  const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = m < modes;
+  int ki[3] = {0, 0, 0};
+  {
+    long long mm = valid ? m : 0;
+    for (int d = DIM - 1; d >= 0; --d) {
+      const int idx = (int)(mm % n);
+      mm /= n;
+      ki[d] = idx;  // index in [0, n); frequency kfull(idx, n)
+    }
+  }
+  double acc[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  for (long long base = 0; base < np; base += 128) {
+    const int cnt = (int)min((long long)128, np - base);
+    __syncthreads();
+    // phase tables: thread i fills particle i
+    if ((int)threadIdx.x < cnt) {
+      const long long j = base + threadIdx.x;
+      for (int d = 0; d < DIM; ++d) {
+        const double x = r[j * DIM + d];
+        for (int i = 0; i < n; ++i) {
+          double sn, cs;
+          sincos(-(double)kfull(i, n) * x, &sn, &cs);
+          sh[((long long)threadIdx.x * DIM + d) * n + i] = make_float2((float)cs, (float)sn);
+        }
+      }
+      for (int c = 0; c < 3; ++c) su[threadIdx.x][c] = c < ncomp ? (float)u_r[j * ncomp + c] : 0.f;
+    }
+    __syncthreads();
+    if (valid) {
+      float tacc[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      for (int q = 0; q < cnt; ++q) {
+        float2 ph = sh[((long long)q * DIM + 0) * n + ki[0]];
+        for (int d = 1; d < DIM; ++d) {
+          const float2 b = sh[((long long)q * DIM + d) * n + ki[d]];
+          ph = make_float2(ph.x * b.x - ph.y * b.y, ph.x * b.y + ph.y * b.x);
+        }
+        for (int c = 0; c < 3; ++c) {
+          tacc[c][0] = fmaf(su[q][c], ph.x, tacc[c][0]);
+          tacc[c][1] = fmaf(su[q][c], ph.y, tacc[c][1]);
+        }
+      }
+      for (int c = 0; c < 3; ++c) {
+        acc[c][0] += tacc[c][0];
+        acc[c][1] += tacc[c][1];
+      }
+    }
+  }
+  if (valid)
+    for (int c = 0; c < 3; ++c) S[c * scs + m] = make_float2((float)acc[c][0], (float)acc[c][1]);
+}
+
 // shift_fn(r, dr) = (r + scale * dr) mod box (integrator.py:21-23), elementwise
 __global__ void k_shift(const double* __restrict__ r, const double* __restrict__ dr, long long n, double scale,
                         double box, double* __restrict__ out) {
@@ -285,6 +352,7 @@ struct l3es_interp_plan {
   float2* g = nullptr;       // [3][n^dim]
   float* gre = nullptr;      // [3][n^dim]
   float* inv_psi = nullptr;  // [c]
+  float2* twc = nullptr;     // c-point twiddles (particle -> grid inverse transform)
   int* count = nullptr;      // [nb^dim]
   int* start = nullptr;      // [nb^dim]
   int* perm = nullptr;       // [np_max]
@@ -312,6 +380,24 @@ static void ip_free(l3es_interp_plan* p) {
   p->coarse = nullptr;
 }
 
+// inverse c2c of a full 3-component grid of NG^dim complex values (g, in place for
+// the strided axes), real part times scale into gre
+template <int NG>
+static void c2c_inverse_re(int dim, float2* g, float* gre, const float2* tw, float scale, cudaStream_t s) {
+  using KY = KyCfg<NG>;
+  constexpr int TX = KY::THREADS, TWY = KY::TWY;
+  const long long per = dim == 3 ? (long long)NG * NG * NG : (long long)NG * NG;
+  if (dim == 3) {
+    ky_pass<NG, kInv><<<dim3((NG * NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(g, per, NG * NG, NG * NG, NG / 2, tw);
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, NG, 3), TX, 0, s>>>(g, per, NG, NG, NG / 2, tw);
+  } else {
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(g, per, NG, NG, NG / 2, tw);
+  }
+  const long long lines = 3 * per / NG;
+  constexpr int LPC = (32 / Fft<NG>::T) * 4;
+  line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(g, gre, lines, tw, scale);
+}
+
 // strided c2c passes of the NUFFT grid (inverse), via the ky_pass kernel
 template <int NG>
 static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
@@ -328,7 +414,7 @@ static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
   }
   const long long lines = 3 * per / NG;
   constexpr int LPC = (32 / Fft<NG>::T) * 4;
-  line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->g, p->gre, lines, p->tw);
+  line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->g, p->gre, lines, p->tw, 1.0f);
 }
 
 static int run_grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
@@ -374,6 +460,7 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   rc = rc ? rc : ip_alloc(p, (void**)&p->g, sizeof(float2) * 3 * p->gcs, "nufft grid");
   rc = rc ? rc : ip_alloc(p, (void**)&p->gre, sizeof(float) * 3 * p->gcs, "nufft grid re");
   rc = rc ? rc : ip_alloc(p, (void**)&p->inv_psi, sizeof(float) * ckp_n, "deconvolution");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->twc, sizeof(float2) * ckp_n, "coarse twiddles");
   rc = rc ? rc : ip_alloc(p, (void**)&p->count, sizeof(int) * nbins, "bins");
   rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * nbins, "bin starts");
   rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * (np_max > 0 ? np_max : 1), "permutation");
@@ -410,8 +497,14 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
     }
     ipsi[i] = (float)(1.0 / ((double)width / (2.0 * p->n) * sum));
   }
+  std::vector<float2> twc(ckp_n);
+  for (int m = 0; m < ckp_n; ++m) {
+    const double a = -2.0 * pi * m / ckp_n;
+    twc[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
   cudaError_t e = cudaMemcpy(p->tw, tw.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->inv_psi, ipsi.data(), sizeof(float) * ckp_n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->twc, twc.data(), sizeof(float2) * ckp_n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     rc = cuda_check(e, "l3es_interp_plan_create");
     ip_free(p);
@@ -516,6 +609,36 @@ int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, i
   }
 #undef L3ES_GATHER
   return cuda_check(cudaGetLastError(), "l3es_interp launch");
+}
+
+int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const double* u_r, int64_t np,
+                                  float* u_grid, void* stream) {
+  if (!p || !r || !u_r || !u_grid) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: null argument");
+  if (np < 0) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: np < 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int c = p->c;
+  const long long modes = p->dim == 3 ? (long long)c * c * c : (long long)c * c;
+  // the NUFFT grid buffers (n = 2c) hold the c^dim spectrum and its real transform
+  const size_t smem = sizeof(float2) * 128 * p->dim * c;
+  if (smem > 200 * 1024) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: grid too large");
+  if (p->dim == 3) {
+    cudaFuncSetAttribute(k_p2g_dft<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_p2g_dft<3><<<(unsigned)((modes + 127) / 128), 128, smem, s>>>(r, u_r, np, 3, c, p->g, modes);
+  } else {
+    cudaFuncSetAttribute(k_p2g_dft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_p2g_dft<2><<<(unsigned)((modes + 127) / 128), 128, smem, s>>>(r, u_r, np, 2, c, p->g, modes);
+  }
+  // u_grid = real(ifftn(S)) (ifftn carries 1/c^dim)
+  const float scale = (float)(1.0 / (double)modes);
+  switch (c) {
+    case 8: c2c_inverse_re<8>(p->dim, p->g, u_grid, p->twc, scale, s); break;
+    case 16: c2c_inverse_re<16>(p->dim, p->g, u_grid, p->twc, scale, s); break;
+    case 32: c2c_inverse_re<32>(p->dim, p->g, u_grid, p->twc, scale, s); break;
+    case 64: c2c_inverse_re<64>(p->dim, p->g, u_grid, p->twc, scale, s); break;
+    case 128: c2c_inverse_re<128>(p->dim, p->g, u_grid, p->twc, scale, s); break;
+    default: return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: unsupported grid");
+  }
+  return cuda_check(cudaGetLastError(), "l3es_interp_particles_to_grid launch");
 }
 
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box, double* out, void* stream) {

@@ -52,6 +52,7 @@ _SIGNATURES = {
     "l3es_interp_coarse_spectrum": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
+    "l3es_interp_particles_to_grid": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_last_error": (ctypes.c_char_p, []),
     "l3es_version": (ctypes.c_char_p, []),
@@ -310,6 +311,16 @@ class InterpPlan:
             raise ValueError(f"expected (np, {self.dim}) arrays")
         _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend], float(dt),
                                      _ptr(r_out), _stream(stream)), "l3es_interp")
+
+    def particles_to_grid(self, r, u_r, out, stream=None) -> None:
+        """real(ifftn(sum_j u_r[j] exp(-i k.r_j))) on the c^dim grid into out (float32,
+        (3, c, c, c) or (3, c, c))."""
+        import torch
+
+        if r.dtype != torch.float64 or u_r.dtype != torch.float64:
+            raise ValueError("positions and velocities are float64 (np, dim)")
+        _check(self._lib.l3es_interp_particles_to_grid(self._h, _ptr(r), _ptr(u_r), int(r.shape[0]), _ptr(out),
+                                                       _stream(stream)), "l3es_interp_particles_to_grid")
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -125,6 +125,12 @@ def install() -> None:
             get_backend=lambda: types.SimpleNamespace(platform="cpu")
         )
     )
+    jsp = types.ModuleType("jax.scipy")
+    jsp.special = types.ModuleType("jax.scipy.special")
+    import math
+
+    jsp.special.factorial = lambda n, exact=False: float(math.factorial(int(n)))
+    jax.scipy = jsp
     exp = types.ModuleType("jax.experimental")
     exp.serialize_executable = types.ModuleType("jax.experimental.serialize_executable")
     jax.experimental = exp
@@ -136,6 +142,8 @@ def install() -> None:
         "jax.random": jax.random,
         "jax.ops": jax.ops,
         "jax.experimental": exp,
+        "jax.scipy": jsp,
+        "jax.scipy.special": jsp.special,
         "jax.experimental.serialize_executable": exp.serialize_executable,
     }.items():
         sys.modules[name] = mod

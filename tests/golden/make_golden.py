@@ -136,6 +136,19 @@ def main(ref_root: str) -> None:
                          ur3=A(i3(g3, r3)), ur2=A(i2(g2, r2)),
                          dr=dr, shifted=A(itg.shift_fn(r3, dr)))
 
+    # --- 8. particle -> grid exact DFT and its spectrum (turbulence.py:299-377) ----
+    tb = importlib.import_module("l3es.turbulence")
+    c3, c2 = 8, 16
+    rp3 = rng.uniform(0, 2 * np.pi, (c3**3, 3))
+    up3 = rng.standard_normal((c3**3, 3))
+    rp2 = rng.uniform(0, 2 * np.pi, (c2**2, 2))
+    up2 = rng.standard_normal((c2**2, 2))
+    g3 = A(tb.ur_to_u_dft_wrapper(c3, 2 * np.pi, 3, (1, 2, 3))(rp3, up3))
+    g2 = A(tb.ur_to_u_dft_wrapper(c2, 2 * np.pi, 2, (1, 2))(rp2, up2))
+    ug3, ek3 = tb.u_and_spectrum_from_ur(c3, 2 * np.pi, 3, "dft", (1, 2, 3))(rp3, up3)
+    out["p2g"] = dict(c3=c3, c2=c2, r3=rp3, u3=up3, r2=rp2, u2=up2, grid3=g3, grid2=g2,
+                      ugrid3=A(ug3), ek3=A(ek3))
+
     for name, d in out.items():
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})

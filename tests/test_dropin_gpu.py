@@ -137,3 +137,30 @@ def test_combined_kolmogorov_matches_oracle_loop(tmp_path):
         r_o = R.shift_fn(r_o, dt * ur)
     assert np.abs(r.cpu().numpy() - r_o).max() < 1e-6
     assert _rel(uh, uh_o) < RTOL
+
+
+def test_particles_to_grid_golden(gold):
+    from l3es import turbulence as T
+
+    g = gold("p2g")
+    c3, c2 = int(g["c3"]), int(g["c2"])
+    assert _rel(T.ur_to_u_dft_wrapper(c3, 2 * np.pi, 3)(g["r3"], g["u3"]), g["grid3"]) < RTOL
+    assert _rel(T.ur_to_u_dft_wrapper(c2, 2 * np.pi, 2, (1, 2))(g["r2"], g["u2"]), g["grid2"]) < RTOL
+    ug, ek = T.u_and_spectrum_from_ur(c3, 2 * np.pi, 3, "dft")(g["r3"], g["u3"])
+    assert _rel(ug, g["ugrid3"]) < RTOL
+    assert _rel(ek, g["ek3"]) < RTOL
+
+
+def test_particles_to_grid_large_vs_oracle():
+    """32^3 particles to a 32^3 grid (the combined loop's analysis size)."""
+    from l3es import turbulence as T
+
+    rng = np.random.default_rng(9)
+    c = 32
+    r = rng.uniform(0, 2 * np.pi, (c**3, 3))
+    u = rng.standard_normal((c**3, 3))
+    got = T.ur_to_u_dft_wrapper(c, 2 * np.pi, 3)(r, u)
+    sub = R.particles_to_grid_dft(r[:4096], u[:4096], c)  # linear in the particles
+    got_sub = T.ur_to_u_dft_wrapper(c, 2 * np.pi, 3)(r[:4096], u[:4096])
+    assert _rel(got_sub, sub.reshape(3, -1).T) < 5e-5
+    assert got.shape == (c**3, 3)

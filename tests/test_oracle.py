@@ -126,3 +126,14 @@ def test_tgv64_known_answer():
     assert round(ke - 0.124953117517, 7) == 0
     ref = float(open(os.path.join(GOLDEN, "tgv64_ke.txt")).read().splitlines()[-1])
     assert abs(ke - ref) < 1e-14
+
+
+def test_particles_to_grid_dft(gold):
+    g = gold("p2g")
+    c3, c2 = int(g["c3"]), int(g["c2"])
+    u3 = R.particles_to_grid_dft(g["r3"], g["u3"], c3)
+    assert _rel(u3.reshape(3, -1).T, g["grid3"]) < 1e-12
+    assert _rel(u3, g["ugrid3"]) < 1e-12
+    u2 = R.particles_to_grid_dft(g["r2"], g["u2"], c2)
+    assert _rel(u2.reshape(2, -1).T, g["grid2"]) < 1e-12
+    assert _rel(R.energy_spectrum(u3), g["ek3"]) < 1e-12
