@@ -190,6 +190,44 @@ int l3es_interp_particles_to_grid(l3es_interp_plan* plan, const double* r, const
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,
                double* out, void* stream);
 
+/* ---- SPH particle relaxation and density ----
+ * Replaces the JAX-SPH neighbour list + quintic kernel + Tait EoS code of
+ * l3es/relax.py:16-178 (relax_wrapper -> loop_body, sph_body) and l3es/utils.py:169-218
+ * (rho_computer). A plan is made for n particles per axis at rest in the periodic box
+ * [0, box)^dim: spacing dx = box / n, mass dx^dim, reference density 1, quintic kernel
+ * of smoothing length dx and cutoff 3 dx, pressure p = p_ref (rho - 1) with
+ * p_ref = (10 u_ref)^2. Positions, velocities and outputs are float64 (np, dim) device
+ * arrays; np <= np_max. Positions are wrapped into the box before use. Outputs depend
+ * only on the inputs (fixed neighbour order), not on the launch. */
+typedef struct l3es_sph_plan l3es_sph_plan;
+int l3es_sph_plan_create(int32_t dim, int32_t n, double box, int64_t np_max, l3es_sph_plan** out);
+int l3es_sph_plan_destroy(l3es_sph_plan* plan);
+
+/* rho_computer(n, dim, box)(r): rho[j] = dx^dim sum_{|r_jk| < 3 dx} W(|r_jk|), the
+ * particle itself included (utils.py:205-216). rho: float64 (np,). */
+int l3es_sph_density(l3es_sph_plan* plan, const double* r, int64_t np, double* rho, void* stream);
+
+/* relax_wrapper(n, dim, box, is_physical, u_ref) loop_body(r) (relax.py:73-120): pressure
+ * plus half the transport-velocity acceleration, in physical units (the reference's
+ * non-dimensional mode returns the same values). */
+int l3es_sph_relax_acceleration(l3es_sph_plan* plan, const double* r, int64_t np, double u_ref,
+                                double* acc, void* stream);
+
+/* relax_wrapper(...) sph_body(r, u) (relax.py:122-176): the pressure, viscous (eta = 1)
+ * and transport-velocity accelerations as three (np, dim) arrays. */
+int l3es_sph_forces(l3es_sph_plan* plan, const double* r, const double* u, int64_t np, double u_ref,
+                    double* acc_p, double* acc_visc, double* acc_tvf, void* stream);
+
+/* The combined loop's relaxation step (combined.py:132-142), fused:
+ *   r_temp = shift(r0, dt u_r); a = loop_body(r_temp);
+ *   r_temp = shift(r_temp, (relax_dt_factor dt)^2 a);
+ *   u_out = periodic_displacement(r_temp, r0) / dt      (minimum image)
+ * and, when r_out != NULL, the loop's advection r_out = shift(r0, dt u_out)
+ * (combined.py:199). Outputs must not alias the inputs. */
+int l3es_sph_relax_velocity(l3es_sph_plan* plan, const double* r0, const double* u_r, int64_t np,
+                            double dt, double relax_dt_factor, double u_ref, double* u_out,
+                            double* r_out, void* stream);
+
 /* ---- CUDA graphs: record library calls once, replay them as one launch ----
  * No counterpart in the reference (its step is one XLA executable per trajectory,
  * spectral_solver.py:130-153). l3es_graph_begin returns a capturing stream; l3es_step,

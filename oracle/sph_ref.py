@@ -50,8 +50,7 @@ def _pairs(r, L, cutoff):
     n = len(r)
     i = np.concatenate([pairs[:, 0], pairs[:, 1], np.arange(n)])
     j = np.concatenate([pairs[:, 1], pairs[:, 0], np.arange(n)])
-    d = r[i] - r[j]
-    d -= L * np.round(d / L)
+    d = periodic_displacement(r[i], r[j], L)
     return i, j, d
 
 
@@ -87,12 +86,48 @@ def relax_acceleration(r, N, dim, u_ref, L=2 * np.pi):
     return out
 
 
+def sph_forces(r, u, N, dim, u_ref, L=2 * np.pi):
+    """relax_wrapper(...).sph_body(r, u) (relax.py:122-176): pressure, viscous (eta 1)
+    and transport-velocity accelerations."""
+    dx = L / N
+    mass = dx**dim
+    p_eos = (10.0 * u_ref) ** 2
+    i, j, d = _pairs(r, L, 3.0 * dx)
+    dist = np.sqrt(np.sum(d * d, axis=1))
+    rho = np.zeros(len(r))
+    np.add.at(rho, i, mass * quintic_w(dist, dx, dim))
+    p = p_eos * (rho - 1.0)
+    dw = quintic_grad_w(dist, dx, dim)
+    grad = dw[:, None] * d / (dist[:, None] + EPS)
+    ri, rj, pi, pj = rho[i], rho[j], p[i], p[j]
+    p_ij = (rj * pi + ri * pj) / (ri + rj)
+    pref = mass * ((1.0 / ri) ** 2 + (1.0 / rj) ** 2)
+    out = {k: np.zeros_like(r) for k in ("acc_p", "acc_visc", "acc_tvf")}
+    np.add.at(out["acc_p"], i, (-pref * p_ij)[:, None] * grad)
+    np.add.at(out["acc_visc"], i, (pref / (dist + EPS) * dw)[:, None] * (u[i] - u[j]))
+    np.add.at(out["acc_tvf"], i, (pref * (-p_eos))[:, None] * grad)
+    return out
+
+
+def periodic_displacement(a, b, L):
+    """jax_md space.periodic displacement: mod(a - b + L/2, L) - L/2."""
+    return np.mod(a - b + 0.5 * L, L) - 0.5 * L
+
+
 def relax_velocity(r0, u_r, dt, relax_dt_factor, N, dim, u_ref, L=2 * np.pi):
     """combined.py:132-142: move to the next positions, one relaxation kick, and the
     velocity that reaches the relaxed positions in one step (minimum image)."""
     r_temp = np.mod(r0 + dt * u_r, L)
     a = relax_acceleration(r_temp, N, dim, u_ref, L)
     r_temp = np.mod(r_temp + (relax_dt_factor * dt) ** 2 * a, L)
-    d = r_temp - r0
+    return periodic_displacement(r_temp, r0, L) / dt
+
+
+def pairs_bruteforce(r, L, cutoff):
+    """Every ordered pair (self included) within the cutoff by an O(n^2) minimum-image
+    scan; an independent check of the tree search above on small inputs."""
+    d = r[:, None, :] - r[None, :, :]
     d -= L * np.round(d / L)
-    return d / dt
+    dist = np.sqrt(np.sum(d * d, axis=2))
+    i, j = np.nonzero(dist < cutoff)
+    return i, j, d[i, j]

@@ -54,6 +54,13 @@ _SIGNATURES = {
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
     "l3es_interp_particles_to_grid": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
+    "l3es_sph_plan_create": (ctypes.c_int, [_I, _I, ctypes.c_double, ctypes.c_int64, ctypes.POINTER(_P)]),
+    "l3es_sph_plan_destroy": (ctypes.c_int, [_P]),
+    "l3es_sph_density": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _P]),
+    "l3es_sph_relax_acceleration": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, _P, _P]),
+    "l3es_sph_forces": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, _P, _P, _P, _P]),
+    "l3es_sph_relax_velocity": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, _P, _P, _P]),
     "l3es_last_error": (ctypes.c_char_p, []),
     "l3es_version": (ctypes.c_char_p, []),
 }
@@ -325,6 +332,64 @@ class InterpPlan:
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.l3es_interp_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SphPlan:
+    """Owns an ``l3es_sph_plan``: cell list and per-particle scratch for n^dim particles
+    in the periodic box [0, box)^dim."""
+
+    def __init__(self, dim: int, n: int, box: float = 2 * 3.141592653589793, np_max: int = 0):
+        lib = load()
+        h = ctypes.c_void_p()
+        np_max = int(np_max) or int(n) ** int(dim)
+        _check(lib.l3es_sph_plan_create(int(dim), int(n), float(box), np_max, ctypes.byref(h)),
+               "l3es_sph_plan_create")
+        self._h, self._lib = h, lib
+        self.dim, self.n, self.box, self.np_max = int(dim), int(n), float(box), np_max
+
+    def _pos(self, *arrays):
+        import torch
+
+        for a in arrays:
+            if a.dtype != torch.float64 or a.dim() != 2 or a.shape[1] != self.dim:
+                raise ValueError(f"expected float64 (np, {self.dim}) arrays")
+            if a.shape[0] != arrays[0].shape[0]:
+                raise ValueError("particle arrays differ in length")
+        return int(arrays[0].shape[0])
+
+    def density(self, r, rho, stream=None) -> None:
+        n = self._pos(r)
+        if rho.numel() != n:
+            raise ValueError("rho must hold one float64 per particle")
+        _check(self._lib.l3es_sph_density(self._h, _ptr(r), n, _ptr(rho), _stream(stream)), "l3es_sph_density")
+
+    def relax_acceleration(self, r, acc, u_ref: float, stream=None) -> None:
+        n = self._pos(r, acc)
+        _check(self._lib.l3es_sph_relax_acceleration(self._h, _ptr(r), n, float(u_ref), _ptr(acc), _stream(stream)),
+               "l3es_sph_relax_acceleration")
+
+    def forces(self, r, u, acc_p, acc_visc, acc_tvf, u_ref: float, stream=None) -> None:
+        n = self._pos(r, u, acc_p, acc_visc, acc_tvf)
+        _check(self._lib.l3es_sph_forces(self._h, _ptr(r), _ptr(u), n, float(u_ref), _ptr(acc_p), _ptr(acc_visc),
+                                         _ptr(acc_tvf), _stream(stream)), "l3es_sph_forces")
+
+    def relax_velocity(self, r0, u_r, u_out, dt: float, relax_dt_factor: float, u_ref: float, r_out=None,
+                       stream=None) -> None:
+        n = self._pos(r0, u_r, u_out) if r_out is None else self._pos(r0, u_r, u_out, r_out)
+        _check(self._lib.l3es_sph_relax_velocity(self._h, _ptr(r0), _ptr(u_r), n, float(dt), float(relax_dt_factor),
+                                                 float(u_ref), _ptr(u_out), _ptr(r_out), _stream(stream)),
+               "l3es_sph_relax_velocity")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.l3es_sph_plan_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -7,9 +7,13 @@ particles move by an explicit Euler shift. On the GPU the coarsening is taken
 directly from the fine spectrum and the interpolation and shift are fused
 (l3es_interp_set_spectrum + l3es_interp with r_out).
 
-Outside this package: SPH relaxation (relax_dt_factor > 0 raises), the SPH density
-column (written empty) and plots. Particle checkpoints go to step_XXXXX.npz files
-with the reference's keys r and u (the reference writes h5 through JAX-SPH).
+With relax_dt_factor > 0 the interpolated velocity is relaxed by one SPH step at the
+predicted positions (combined.py:132-142) in one fused call (l3es_sph_relax_velocity,
+which also advects the particles with the relaxed velocity). The SPH density maximum
+is logged on log/checkpoint steps as in the reference. Outside this package: plots.
+Particle checkpoints go to step_XXXXX.npz files with the reference's keys r and u (the
+unrelaxed interpolated velocity, as the reference writes; the reference writes h5
+through JAX-SPH).
 """
 
 from __future__ import annotations
@@ -21,6 +25,7 @@ from time import time
 import numpy as np
 
 from .integrator import set_up_integrator
+from .relax import relax_velocity_wrapper
 from .spectral_solver import _field_stats, dt_from_stats, set_up_solver, _torch
 from .utils import _interp_plan, write_u
 
@@ -31,8 +36,6 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
              dst_path=None, **ext):
     """Integrate particles along the DNS velocity (combined.py:18-219). Returns the final
     (u, u_hat, r)."""
-    if relax_dt_factor and relax_dt_factor > 0.0:
-        raise NotImplementedError("SPH relaxation (relax_dt_factor > 0) is not part of this package")
     torch = _torch()
     dst_path = dst_path or "results"
     int_path = os.path.join(dst_path, "com")
@@ -45,9 +48,10 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
         N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target, forcing_type, rejit, **ext)
     print(f"{'#' * 79}\nSimulation with N={N}, nu={nu}, t_final={t_final}, dt={dt}",
           f"E_kin_init={ek_ini:.3f}\n{'#' * 79}")
-    r, _, _, _, _, _, _ = set_up_integrator(state_0_path, dim, ckp_N, dft_splits, u_ref, interp_backend)
+    r, comp_rho, _, _, _, _, _ = set_up_integrator(state_0_path, dim, ckp_N, dft_splits, u_ref, interp_backend)
     npart = r.shape[0]
     ip = _interp_plan(dim, N, ckp_N, np_max=npart)
+    relax = relax_velocity_wrapper(ckp_N, dim, L, u_ref, relax_dt_factor) if (relax_dt_factor or 0.0) > 0.0 else None
     u_r = torch.empty_like(r)
     r_next = torch.empty_like(r)
     e_acc = torch.zeros((), dtype=torch.float64, device="cuda")
@@ -71,19 +75,27 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
         # u_lres = spectral_filtering(u_hres, ckp_N); u_r = interpolator(u_lres, r);
         # r_next = shift_fn(r, dt * u_r)   (combined.py:122-130, :199)
         ip.set_spectrum(u_hat)
-        ip.interp(r, u_r, backend=interp_backend, dt=dt, r_out=r_next)
+        if relax is None:
+            ip.interp(r, u_r, backend=interp_backend, dt=dt, r_out=r_next)
+        else:
+            # u_r_0 kept for the checkpoint; particles advance with the relaxed velocity
+            ip.interp(r, u_r, backend=interp_backend)
+            relax(r, u_r, dt, r_out=r_next)
         torch.cuda.synchronize()
         t_int += time() - t_temp
 
         is_ckp = (i % ckp_freq == 0) and (i >= burnin_steps)
+        rho_max = ""
+        if i % log_freq == 0 or is_ckp or i % vis_freq == 0:
+            rho_max = float(comp_rho(r).max())
         if i % log_freq == 0:
             st = _field_stats(u, dim).cpu().numpy()
             umax, e_kin = float(st[:3].max()), float(st[3])
             dt_est = float(dt_from_stats(st, dx_dns, nu))
             with open(diagnostics_path, "a", newline="") as f:
-                csv.writer(f).writerow([i, float(i * dt), umax, e_kin, dt_est, float(e_inj), ""])
+                csv.writer(f).writerow([i, float(i * dt), umax, e_kin, dt_est, float(e_inj), rho_max])
             print(f"Step {i}/{tstep_max}, u_max = {umax:.3f}, E_kin = {e_kin:.3f}, "
-                  f"dt_est = {dt_est:.5f}, E_inj = {float(e_inj):.3f}")
+                  f"dt_est = {dt_est:.5f}, E_inj = {float(e_inj):.3f}, rho_max = {rho_max:.3f}")
         if is_ckp:
             np.savez(os.path.join(int_path, f"step_{i:05d}.npz"), r=r.cpu().numpy(), u=u_r.cpu().numpy())
         r, r_next = r_next, r

@@ -1,8 +1,8 @@
 """Particle interpolation and advection: drop-in for the hot-path part of
 l3es/integrator.py (``shift_fn``, ``spectral_interpolator_wrapper``,
 ``set_up_integrator``). Positions and velocities are float64 (np, dim) torch CUDA
-tensors, as the reference keeps them in FP64. SPH relaxation and density
-(relax_wrapper, rho_computer) are outside this package.
+tensors, as the reference keeps them in FP64. ``set_up_integrator`` also returns the
+SPH density and relaxation functions (l3es.utils.rho_computer, l3es.relax.relax_wrapper).
 """
 
 from __future__ import annotations
@@ -64,9 +64,12 @@ def pos_init_cartesian(L, n, dim):
 
 def set_up_integrator(state_0_path, dim, N, dft_splits, u_ref, interp_backend):
     """integrator.py:96-114. Returns the reference's 7-tuple
-    (r, comp_rho, interpolator, relax_fn, sph_fn, L, fft_axes); the SPH entries
-    (comp_rho, relax_fn, sph_fn) are None. state_0_path may name a .npy/.npz file
-    holding the initial positions (the reference reads an h5 written by JAX-SPH)."""
+    (r, comp_rho, interpolator, relax_fn, sph_fn, L, fft_axes). state_0_path may name a
+    .npy/.npz file holding the initial positions (the reference reads an h5 written by
+    JAX-SPH)."""
+    from .relax import relax_wrapper
+    from .utils import rho_computer
+
     torch = _torch()
     L = 2 * np.pi
     fft_axes = (1, 2, 3) if dim == 3 else (1, 2)
@@ -77,4 +80,6 @@ def set_up_integrator(state_0_path, dim, N, dft_splits, u_ref, interp_backend):
         r = pos_init_cartesian(L, N, dim)
     r = torch.as_tensor(np.asarray(r, dtype=np.float64), device="cuda")
     interpolator = spectral_interpolator_wrapper(N, fft_axes, splits=dft_splits or 1, backend=interp_backend)
-    return r, None, interpolator, None, None, L, fft_axes
+    comp_rho = rho_computer(N, dim=dim, L=L)
+    relax_fn, sph_fn = relax_wrapper(N, dim, L, is_physical=True, u_ref=u_ref)
+    return r, comp_rho, interpolator, relax_fn, sph_fn, L, fft_axes

@@ -1,10 +1,11 @@
 """Spectral utilities: drop-in for the hot-path part of l3es/utils.py.
 
 ``spectral_filtering``, ``energy_spectrum``, ``comp_dissipation_rate``,
-``get_real_wavenumber_grid`` and ``write_u`` with the reference's arguments. Fields
-are torch CUDA tensors (NumPy arrays are accepted and moved to the GPU); the work
-runs in the CUDA library. SPH density, finite-difference vorticity/divergence and
-the incompressible projections of the reference module are outside this package.
+``get_real_wavenumber_grid``, ``write_u`` and the SPH density ``rho_computer`` with the
+reference's arguments. Fields are torch CUDA tensors (NumPy arrays are accepted and
+moved to the GPU); the work runs in the CUDA library. Finite-difference
+vorticity/divergence and the incompressible projections of the reference module are
+outside this package.
 """
 
 from __future__ import annotations
@@ -121,3 +122,21 @@ def write_u(u, tstep, dst_path, ckp_N, suffix=""):
     os.makedirs(dst_path, exist_ok=True)
     arr = y.detach().cpu().numpy() if hasattr(y, "detach") else np.asarray(y)
     np.save(os.path.join(dst_path, f"u_{ckp_N}_{tstep:05d}{suffix}.npy"), arr)
+
+
+def rho_computer(N, dim=3, L=2 * np.pi):
+    """utils.py:169-218: returns comp_rho(r) -> SPH density (np,) float64 of the
+    particles at r (quintic kernel, h = L/N, cutoff 3h, mass (L/N)^dim, the particle
+    itself included)."""
+    from .relax import _SphPlans, _pos
+
+    plans = _SphPlans(N, dim, L)
+    torch = _torch()
+
+    def comp_rho(r):
+        r = _pos(r)
+        rho = torch.empty(r.shape[0], dtype=torch.float64, device="cuda")
+        plans.get(r.shape[0]).density(r, rho)
+        return rho
+
+    return comp_rho

@@ -137,3 +137,60 @@ def test_particles_to_grid_dft(gold):
     u2 = R.particles_to_grid_dft(g["r2"], g["u2"], c2)
     assert _rel(u2.reshape(2, -1).T, g["grid2"]) < 1e-12
     assert _rel(R.energy_spectrum(u3), g["ek3"]) < 1e-12
+
+
+def _lattice(n, dim, jitter=0.0, seed=0):
+    L = 2 * np.pi
+    r = R.pos_init_cartesian(L, n, dim)
+    if jitter:
+        r = np.mod(r + jitter * (L / n) * np.random.default_rng(seed).uniform(-1, 1, r.shape), L)
+    return r
+
+
+def test_sph_quintic_normalisation():
+    """The restated quintic constants: the 2D kernel integrates to 1; the 3D constant
+    3/(359 pi) of the published kernel integrates to 360/359."""
+    from scipy.integrate import quad
+
+    from oracle import sph_ref as S
+
+    h = 0.37
+    i2 = quad(lambda r: 2 * np.pi * r * S.quintic_w(r, h, 2), 0, 3 * h, points=[h, 2 * h])[0]
+    i3 = quad(lambda r: 4 * np.pi * r * r * S.quintic_w(r, h, 3), 0, 3 * h, points=[h, 2 * h])[0]
+    assert abs(i2 - 1.0) < 1e-12 and abs(i3 - 360 / 359) < 1e-12
+    q = np.linspace(0.01, 2.99, 50)
+    num = (S.quintic_w(q + 1e-6, 1.0, 3) - S.quintic_w(q - 1e-6, 1.0, 3)) / 2e-6
+    assert np.abs(num - S.quintic_grad_w(q, 1.0, 3)).max() < 1e-6 * np.abs(num).max()
+
+
+@pytest.mark.parametrize("n,dim", [(8, 3), (12, 2)])
+def test_sph_tree_search_matches_bruteforce(n, dim):
+    from oracle import sph_ref as S
+
+    r = _lattice(n, dim, jitter=0.4, seed=1)
+    L, cut = 2 * np.pi, 3 * 2 * np.pi / n
+    i, j, d = S._pairs(r, L, cut)
+    bi, bj, bd = S.pairs_bruteforce(r, L, cut)
+    a = sorted(zip(i.tolist(), j.tolist()))
+    assert a == sorted(zip(bi.tolist(), bj.tolist()))
+    key = {(x, y): k for k, (x, y) in enumerate(zip(bi.tolist(), bj.tolist()))}
+    order = [key[(x, y)] for x, y in zip(i.tolist(), j.tolist())]
+    assert np.abs(d - bd[order]).max() < 1e-12
+
+
+@pytest.mark.parametrize("n,dim", [(16, 3), (32, 2)])
+def test_sph_lattice_and_momentum(n, dim):
+    """A lattice has uniform density and no net acceleration; the pair forces of a
+    jittered set are antisymmetric, so they sum to zero."""
+    from oracle import sph_ref as S
+
+    rho = S.density(_lattice(n, dim), n, dim)
+    assert np.ptp(rho) < 1e-12 and abs(rho.mean() - (1.0027654191593 if dim == 3 else 1.0000632245946)) < 1e-9
+    assert np.abs(S.relax_acceleration(_lattice(n, dim), n, dim, 4.0)).max() < 1e-9
+    r = _lattice(n, dim, jitter=0.3, seed=2)
+    a = S.relax_acceleration(r, n, dim, 4.0)
+    assert np.abs(a.sum(0)).max() < 1e-9 * np.abs(a).max() * len(r)
+    u = np.random.default_rng(3).standard_normal(r.shape)
+    f = S.sph_forces(r, u, n, dim, 4.0)
+    np.testing.assert_allclose(f["acc_p"] + 0.5 * f["acc_tvf"], a, rtol=0, atol=1e-9 * np.abs(a).max())
+    assert np.abs(f["acc_visc"].sum(0)).max() < 1e-9 * np.abs(f["acc_visc"]).max() * len(r)
