@@ -190,6 +190,33 @@ int l3es_interp_particles_to_grid(l3es_interp_plan* plan, const double* r, const
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box,
                double* out, void* stream);
 
+/* ---- Reverse mode (gradients through the RK4 step) ----
+ * The reference obtains these derivatives with jax.grad of its step
+ * (l3es/spectral_solver.py:50-80); here they are hand-written vector-Jacobian
+ * products. Gradients of a real loss L with respect to a complex64 half spectrum z
+ * use the convention dL/dRe z + i dL/dIm z (PyTorch's), i.e.
+ * dL = Re sum(conj(grad) dz) over the stored entries. Supported forcings: none and
+ * const_power (with drag and the Kolmogorov term); ekin_tot returns L3ES_EINVAL.
+ * The first call allocates the plan's adjoint workspace (10 spectra of the plan's
+ * size); l3es_plan_adjoint_prepare does it ahead of time (before any capture). */
+int l3es_plan_adjoint_prepare(l3es_plan* plan);
+
+/* out = (d rhs / d u_hat)^T g at u_hat (the adjoint of l3es_rhs). */
+int l3es_rhs_vjp(l3es_plan* plan, const void* u_hat, const void* g, void* out, void* stream);
+
+/* One step backwards: lam holds dL/du_hat_{n+1} on entry and dL/du_hat_n on return,
+ * u_hat_n is the state at the start of the step (the caller's checkpoint; not
+ * modified). The inner RK4 stages are recomputed from it. */
+int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* stream);
+
+/* Loss on the plan's coarse grid, L = mean((spectral_filtering(irfftn(u_hat_fine), c)
+ * - target)^2) over the dim velocity components (utils.py:100-138 for the
+ * coarsening), into loss_dev (one double), and, when grad != NULL, dL/du_hat_fine
+ * (complex64, the fine spectrum's shape). target: float32 (dim, c, c[, c]). The plan
+ * must have been created with n_fine > 0. */
+int l3es_interp_coarse_mse(l3es_interp_plan* plan, const void* u_hat_fine, const float* target,
+                           double* loss_dev, void* grad, void* stream);
+
 /* ---- SPH particle relaxation and density ----
  * Replaces the JAX-SPH neighbour list + quintic kernel + Tait EoS code of
  * l3es/relax.py:16-178 (relax_wrapper -> loop_body, sph_body) and l3es/utils.py:169-218

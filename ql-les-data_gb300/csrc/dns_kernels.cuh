@@ -147,7 +147,7 @@ ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
     for (int e = 0; e < E; ++e) {
       const int ky = t + T * e;
       const int k = kfull(ky, N);
-      if (k <= kd_store && -k <= kd_store) base[(long long)ky * row] = v[e];
+      if ((unsigned)(k + kd_store) <= 2u * (unsigned)kd_store) base[(long long)ky * row] = v[e];  // |k| <= kd_store
     }
   }
 }
@@ -531,7 +531,7 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int kx = kfull(t + T * e, N);
-    if (kx > kd || -kx > kd) continue;
+    if ((unsigned)(kx + kd) > 2u * (unsigned)kd) continue;  // |kx| > kd
     float k0, k1, k2;
     kvec<DIM>(kx, km, kh, k0, k1, k2);
     const bool keep = kh <= kd;

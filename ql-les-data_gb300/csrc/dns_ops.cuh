@@ -115,6 +115,54 @@ struct DnsOps {
     else
       rfftn_dim<2>(c, u, uh, s);
   }
+
+  // Vector-Jacobian product of the RHS (adjoint_kernels.cuh): u/curl x-inverse,
+  // projected-cotangent x-inverse (+ band terms), y inverse (3D), one line pass for
+  // both products, y forward (3D), x forward, elementwise epilogue.
+  template <int DIM>
+  static void vjp_dim(const Ctx& c, const AdjEpi& a, float2* Wm, float2* Y6, cudaStream_t s) {
+    const long long mc = c.nmid * H;
+    const long long lines = c.nmid * N;
+    const float scale = (float)(1.0 / (DIM == 3 ? (double)N * N * N : (double)N * N));
+    const double A = 8.0 * 3.0 * c.cs * c.batch;  // bytes of one 3-component spectrum
+    const unsigned xb = (unsigned)((mc + TW - 1) / TW);
+    const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
+    L3ES_LAUNCH(c, KK_X_INV, 3.0 * A, s,
+                kx_inv<N, DIM, true><<<dim3(xb, c.batch), TX, 0, s>>>(a.us, c.cs, c.W, c.fs, c.tw));
+    L3ES_LAUNCH(c, KK_ADJ_X_INV, 2.0 * A, s,
+                kx_inv_adjproj<N, DIM><<<dim3(xb, c.batch), TX, 0, s>>>(
+                    a.g, c.cs, a.gscale, c.kd, Wm, c.fs, c.tw, a.us, a.band_kf2 > 0 ? c.kf : 0, inv_n2d,
+                    c.eps_inj, const_cast<double*>(a.band_adj)));
+    if (DIM == 3) {
+      L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
+                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H,
+                                                                                         N / 2, c.tw));
+      L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
+                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(Wm, c.fs, H, H, N / 2,
+                                                                                         c.tw));
+    }
+    L3ES_LAUNCH(c, KK_ADJ_LINE, 5.0 * A, s,
+                line_cross_adj<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
+                    Wm, c.W, c.fs, Y6, c.cs, scale, c.tw, (int)lines));
+    if (DIM == 3)
+      L3ES_LAUNCH(c, KK_Y_FWD, 4.0 * A, s,
+                  ky_pass<N, kFwd><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(Y6, c.cs, H, H, N / 2,
+                                                                                         c.tw));
+    // Y6 (6 fields per trajectory) -> W, as 2 * batch groups of 3 fields
+    L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 4.0 * A, s,
+                kx_fwd_plain<N, DIM><<<dim3(xb, 2 * c.batch), TX, 0, s>>>(Y6, c.cs, c.W, c.fs, c.tw));
+    const long long pairs = c.cs / 2;
+    L3ES_LAUNCH(c, KK_ADJ_EPI, (a.lam_in ? 7.0 : 6.0) * A + (a.g_out ? A : 0.0), s,
+                k_adj_epi<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(c.W, c.cs, a,
+                                                                                                 c.nu_b));
+  }
+
+  static void vjp(const Ctx& c, const AdjEpi& a, float2* Wm, float2* Y6, cudaStream_t s) {
+    if (c.dim == 3)
+      vjp_dim<3>(c, a, Wm, Y6, s);
+    else
+      vjp_dim<2>(c, a, Wm, Y6, s);
+  }
 };
 
 template <int N>
@@ -124,6 +172,7 @@ DnsTable make_dns_table() {
   t.stage = &DnsOps<N>::stage;
   t.irfftn = &DnsOps<N>::irfftn;
   t.rfftn = &DnsOps<N>::rfftn;
+  t.vjp = &DnsOps<N>::vjp;
   return t;
 }
 

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/l3es_gb300.h"
+#include "adjoint_kernels.cuh"
 #include "dns_kernels.cuh"
 
 namespace l3es {
@@ -32,6 +33,9 @@ enum KernelKind {
   KK_NUFFT_GATHER,  // NUFFT gather + advection
   KK_PARTICLE_SORT, // particle binning
   KK_RK_UPDATE,     // k_rk_update (elementwise RK4 combination)
+  KK_ADJ_X_INV,     // kx_inv_adjproj (projected cotangent, x inverse, band terms)
+  KK_ADJ_LINE,      // line_cross_adj (both adjoint products)
+  KK_ADJ_EPI,       // k_adj_epi (vjp assembly + RK4 reverse recursion)
   KK_COUNT
 };
 const char* kernel_kind_name(int k);
@@ -142,7 +146,38 @@ struct DnsTable {
                 cudaStream_t s);
   void (*irfftn)(const Ctx&, const float2* uh, float* u, cudaStream_t s);
   void (*rfftn)(const Ctx&, const float* u, float2* uh, cudaStream_t s);
+  // vector-Jacobian product of the RHS at a.us with cotangent a.gscale * a.g, folded
+  // into the RK4 reverse recursion (AdjEpi); Wm: [batch][3][cs], Y6: [batch][6][cs]
+  void (*vjp)(const Ctx&, const AdjEpi& a, float2* Wm, float2* Y6, cudaStream_t s);
 };
+
+// Adjoint scratch of a plan, allocated by the first adjoint call.
+struct AdjWork {
+  float2* Ua = nullptr;   // [batch][3][cs] RK stage states recomputed from the checkpoint
+  float2* Ub = nullptr;
+  float2* Uc = nullptr;
+  float2* Wm = nullptr;   // [batch][3][cs] projected cotangent lines
+  float2* Y6 = nullptr;   // [batch][6][cs] product spectra
+  float2* LAM = nullptr;  // [batch][3][cs] accumulated cotangent
+  float2* G = nullptr;    // [batch][3][cs] stage cotangent
+  double* band = nullptr; // [batch][2]
+  std::vector<void*> allocs;
+};
+
+}  // namespace l3es
+
+struct l3es_plan {
+  l3es_plan_desc desc;
+  l3es::Ctx ctx;
+  l3es::KTimer timer;
+  l3es::DnsTable tab;
+  int device = 0;
+  long long ws_bytes = 0;
+  std::vector<void*> allocs;
+  l3es::AdjWork adj;
+};
+
+namespace l3es {
 
 // Launch table of grid size N (defined in dns_ops.cuh, instantiated per N in dns_n*.cu).
 template <int N>

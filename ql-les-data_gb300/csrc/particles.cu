@@ -306,6 +306,76 @@ __global__ void k_shift(const double* __restrict__ r, const double* __restrict__
   out[i] = x;
 }
 
+// ------------------------------------------------------------------------------
+// Coarse-grid MSE loss and its gradient with respect to the fine half spectrum.
+// k_mse_resid: in place uc <- 2 (uc - target) / size (components >= ncomp <- 0), FP64
+// per-block partial sums of (uc - target)^2.
+// k_uncrop_grad: G(k) = wt n(k) / (2 N^d) V(k mod c), V = rfftn_c of the residual,
+// n(k) = [k in box] + [-k in box], box = [-c/2, c/2 - 1]^d with fine frequencies in
+// [-N/2, N/2 - 1]: the adjoint of irfftn_c(crop(.)) (the crop averages each coarse
+// mode with the conjugate of its mirror, and irfftn drops the imaginary part of the
+// half-axis planes 0 and N/2, so every stored fine mode inside the box or whose
+// mirror is inside contributes with that mode's multiplicity).
+// ------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_mse_resid(float* __restrict__ uc, const float* __restrict__ tgt, long long per, int ncomp, double inv_size,
+            double* __restrict__ partial) {
+  double acc = 0.0;
+  const long long total = 3 * per;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    float v = 0.f;
+    if (i < ncomp * per) {
+      const double d = (double)uc[i] - (double)tgt[i];
+      acc += d * d;
+      v = (float)(2.0 * d * inv_size);
+    }
+    uc[i] = v;
+  }
+  block_sum_store(acc, partial, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256)
+k_mse_sum(const double* __restrict__ partial, int n, double inv_size, double* __restrict__ out) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+  __shared__ double tot[1];
+  block_sum_store(acc, tot, 0);
+  __syncthreads();
+  if (threadIdx.x == 0) out[0] = tot[0] * inv_size;
+}
+
+__device__ __forceinline__ int signed_freq(int i, int n) { return i < n / 2 ? i : i - n; }
+
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_uncrop_grad(const float2* __restrict__ V, long long hcs, int c, int N, long long cs, int ncomp, float scale,
+              float2* __restrict__ G) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (i >= cs) return;
+  const int H = N / 2 + 1, hc = c / 2 + 1;
+  const int kh = (int)(i % H);
+  const long long rest = i / H;
+  const int mid = DIM == 3 ? (int)(rest % N) : 0;
+  const int xi = DIM == 3 ? (int)(rest / N) : (int)rest;
+  const int lo = -c / 2, hi = c / 2 - 1;
+  const int sx = signed_freq(xi, N), sm = signed_freq(mid, N), sh = signed_freq(kh, N);
+  const int nx = signed_freq((N - xi) % N, N), nm = signed_freq((N - mid) % N, N), nh = signed_freq((N - kh) % N, N);
+  const bool in_k = sx >= lo && sx <= hi && (DIM == 2 || (sm >= lo && sm <= hi)) && sh >= lo && sh <= hi;
+  const bool in_m = nx >= lo && nx <= hi && (DIM == 2 || (nm >= lo && nm <= hi)) && nh >= lo && nh <= hi;
+  const int n = (int)in_k + (int)in_m;
+  float2 out = make_float2(0.f, 0.f);
+  if (n > 0 && comp < ncomp) {
+    const int wt = (kh == 0 || kh == N / 2) ? 1 : 2;
+    const long long ci = DIM == 3 ? ((long long)(xi % c) * c + (mid % c)) * hc + kh : (long long)(xi % c) * hc + kh;
+    const float2 v = V[comp * hcs + ci];
+    const float f = scale * (float)(wt * n);
+    out = make_float2(f * v.x, f * v.y);
+  }
+  G[comp * cs + i] = out;
+}
+
 }  // namespace l3es
 
 using namespace l3es;
@@ -356,6 +426,7 @@ struct l3es_interp_plan {
   int* count = nullptr;      // [nb^dim]
   int* start = nullptr;      // [nb^dim]
   int* perm = nullptr;       // [np_max]
+  double* red = nullptr;     // [1024] loss partial sums
   l3es_plan* coarse = nullptr;  // size-c transforms (irfftn of Hh, rfftn of a coarse field)
   long long hcs = 0, gcs = 0;
   Ctx gctx;                  // geometry for the grid passes (twiddles only)
@@ -464,6 +535,7 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   rc = rc ? rc : ip_alloc(p, (void**)&p->count, sizeof(int) * nbins, "bins");
   rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * nbins, "bin starts");
   rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * (np_max > 0 ? np_max : 1), "permutation");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->red, sizeof(double) * 1024, "loss partials");
   if (rc == L3ES_OK) {
     l3es_plan_desc d{};
     d.dim = dim;
@@ -639,6 +711,35 @@ int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const do
     default: return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: unsupported grid");
   }
   return cuda_check(cudaGetLastError(), "l3es_interp_particles_to_grid launch");
+}
+
+int l3es_interp_coarse_mse(l3es_interp_plan* p, const void* u_hat_fine, const float* target, double* loss_dev,
+                           void* grad, void* stream) {
+  if (!p || !u_hat_fine || !target || !loss_dev) return fail(L3ES_EINVAL, "l3es_interp_coarse_mse: null argument");
+  if (p->n_fine <= 0) return fail(L3ES_ESTATE, "plan was created without a fine grid (n_fine = 0)");
+  if (grad == u_hat_fine) return fail(L3ES_EINVAL, "l3es_interp_coarse_mse: grad must not alias u_hat_fine");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = l3es_interp_set_spectrum(p, u_hat_fine, stream);
+  if (rc == L3ES_OK) rc = l3es_irfftn(p->coarse, p->hh, p->gre, stream);  // coarse field (3, c^d)
+  if (rc != L3ES_OK) return rc;
+  const int c = p->c, N = p->n_fine;
+  const long long per = p->dim == 3 ? (long long)c * c * c : (long long)c * c;
+  const double inv_size = 1.0 / ((double)p->dim * per);
+  const int nblk = (int)std::min<long long>(1024, (3 * per + 255) / 256);
+  k_mse_resid<<<nblk, 256, 0, s>>>(p->gre, target, per, p->dim, inv_size, p->red);
+  k_mse_sum<<<1, 256, 0, s>>>(p->red, nblk, inv_size, loss_dev);
+  rc = cuda_check(cudaGetLastError(), "l3es_interp_coarse_mse launch");
+  if (rc != L3ES_OK || !grad) return rc;
+  rc = l3es_rfftn(p->coarse, p->gre, p->g, stream);  // V = rfftn_c(residual)
+  if (rc != L3ES_OK) return rc;
+  const long long cs = p->dim == 3 ? (long long)N * N * (N / 2 + 1) : (long long)N * (N / 2 + 1);
+  const float scale = (float)(0.5 / std::pow((double)N, p->dim));
+  const dim3 gb((unsigned)((cs + 255) / 256), 3);
+  if (p->dim == 3)
+    k_uncrop_grad<3><<<gb, 256, 0, s>>>(p->g, p->hcs, c, N, cs, 3, scale, (float2*)grad);
+  else
+    k_uncrop_grad<2><<<gb, 256, 0, s>>>(p->g, p->hcs, c, N, cs, 2, scale, (float2*)grad);
+  return cuda_check(cudaGetLastError(), "l3es_interp_coarse_mse launch");
 }
 
 int l3es_shift(const double* r, const double* dr, int64_t n, double scale, double box, double* out, void* stream) {

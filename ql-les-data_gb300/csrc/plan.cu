@@ -9,16 +9,6 @@
 
 #include "l3es_internal.h"
 
-struct l3es_plan {
-  l3es_plan_desc desc;
-  l3es::Ctx ctx;
-  l3es::KTimer timer;
-  l3es::DnsTable tab;
-  int device = 0;
-  long long ws_bytes = 0;
-  std::vector<void*> allocs;
-};
-
 namespace l3es {
 
 static thread_local std::string g_err;
@@ -40,7 +30,8 @@ const char* kernel_kind_name(int k) {
   static const char* names[KK_COUNT] = {
       "kx_inv_curl", "ky_pass_inv", "line_cross", "ky_pass_fwd", "kx_fwd_band", "band_scale",
       "force_ekin", "kx_inv", "line_c2r", "line_r2c", "kx_fwd", "reduce",
-      "filter", "nufft_prep", "nufft_fft", "nufft_gather", "particle_sort", "rk_update"};
+      "filter", "nufft_prep", "nufft_fft", "nufft_gather", "particle_sort", "rk_update",
+      "kx_inv_adjproj", "line_cross_adj", "adj_epilogue"};
   return (k >= 0 && k < KK_COUNT) ? names[k] : "";
 }
 
@@ -139,6 +130,8 @@ static int plan_alloc(l3es_plan* p, void** ptr, size_t bytes, const char* what) 
 static void plan_free(l3es_plan* p) {
   for (void* a : p->allocs) cudaFree(a);
   p->allocs.clear();
+  for (void* a : p->adj.allocs) cudaFree(a);
+  p->adj = AdjWork();
 }
 
 extern "C" {

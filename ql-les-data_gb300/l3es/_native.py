@@ -54,6 +54,10 @@ _SIGNATURES = {
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
     "l3es_interp_particles_to_grid": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
+    "l3es_plan_adjoint_prepare": (ctypes.c_int, [_P]),
+    "l3es_rhs_vjp": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "l3es_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P]),
+    "l3es_interp_coarse_mse": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "l3es_sph_plan_create": (ctypes.c_int, [_I, _I, ctypes.c_double, ctypes.c_int64, ctypes.POINTER(_P)]),
     "l3es_sph_plan_destroy": (ctypes.c_int, [_P]),
     "l3es_sph_density": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _P]),
@@ -199,6 +203,24 @@ class Plan:
         self._check_spec(du)
         _check(self._lib.l3es_rhs(self._h, _ptr(u_hat), _ptr(du), _stream(stream)), "l3es_rhs")
 
+    def adjoint_prepare(self) -> None:
+        """Allocate the adjoint workspace now (before any stream capture)."""
+        _check(self._lib.l3es_plan_adjoint_prepare(self._h), "l3es_plan_adjoint_prepare")
+
+    def rhs_vjp(self, u_hat, g, out, stream=None) -> None:
+        """out = (d rhs / d u_hat)^T g (gradient convention dL/dRe + i dL/dIm)."""
+        self._check_spec(u_hat)
+        self._check_spec(g)
+        self._check_spec(out)
+        _check(self._lib.l3es_rhs_vjp(self._h, _ptr(u_hat), _ptr(g), _ptr(out), _stream(stream)), "l3es_rhs_vjp")
+
+    def adjoint_step(self, u_hat_n, lam, stream=None) -> None:
+        """lam <- (d step / d u_hat_n)^T lam for one RK4 step from the checkpoint u_hat_n."""
+        self._check_spec(u_hat_n)
+        self._check_spec(lam)
+        _check(self._lib.l3es_adjoint_step(self._h, _ptr(u_hat_n), _ptr(lam), _stream(stream)),
+               "l3es_adjoint_step")
+
     def rfftn(self, u, u_hat, stream=None) -> None:
         self._check_phys(u)
         self._check_spec(u_hat)
@@ -318,6 +340,19 @@ class InterpPlan:
             raise ValueError(f"expected (np, {self.dim}) arrays")
         _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend], float(dt),
                                      _ptr(r_out), _stream(stream)), "l3es_interp")
+
+    def coarse_mse(self, u_hat_fine, target, loss, grad=None, stream=None) -> None:
+        """loss[0] = mean((spectral_filtering(irfftn(u_hat_fine), c) - target)^2) and,
+        when grad is given, its gradient with respect to u_hat_fine. Replaces the
+        plan's coarse spectrum."""
+        import torch
+
+        if target.dtype != torch.float32 or target.numel() != self.dim * self.c**self.dim:
+            raise ValueError(f"target must be float32 ({self.dim}, c, ...) with c = {self.c}")
+        if loss.dtype != torch.float64:
+            raise ValueError("loss is a float64 device tensor")
+        _check(self._lib.l3es_interp_coarse_mse(self._h, _ptr(u_hat_fine), _ptr(target), _ptr(loss), _ptr(grad),
+                                                _stream(stream)), "l3es_interp_coarse_mse")
 
     def particles_to_grid(self, r, u_r, out, stream=None) -> None:
         """real(ifftn(sum_j u_r[j] exp(-i k.r_j))) on the c^dim grid into out (float32,

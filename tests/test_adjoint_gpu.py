@@ -1,0 +1,191 @@
+"""Hand-written adjoint on the GPU vs the FP64 adjoint oracle (oracle/adjoint_ref.py,
+itself pinned by finite differences) and vs central finite differences of the GPU
+forward (the 128^3 differentiation workload: 20 RK4 steps, 16 seeded directions).
+
+FP32 transforms put the vector-Jacobian products within ~1e-5 of the FP64 values
+(relative to their largest entry); the tolerances below are written per check.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import adjoint_ref as A
+from oracle import numpy_ref as R
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _c64(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex64)).cuda()
+
+
+def _rel(a, b):
+    a = a.cpu().numpy() if hasattr(a, "cpu") else a
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _state(dim, n, seed, kp=3.0):
+    if dim == 3:
+        u = R.init_u_hit(n, seed, "k4exp", kp)
+        u *= np.sqrt(0.5 / R.kinetic_energy(u))
+        return np.fft.rfftn(u, axes=(1, 2, 3))
+    u = R.init_u_random2d(n, seed)
+    return np.fft.rfftn(u[..., 0] if u.ndim == 4 else u, axes=(1, 2))
+
+
+def _crand(shape, seed, dim, scale=1.0):
+    rng = np.random.default_rng(seed)
+    z = scale * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    if dim == 2:
+        z[2] = 0.0
+    return z
+
+
+def _oracle_fns(dim, n, nu, drag, forced):
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    cp = None
+    if forced:
+        _, kkk2, _, _ = R.wavenumbers(n, dim)
+        cp = (0.1, ((kkk2 > 0) & (kkk2 <= 4)).astype(float))
+    return (axes, R.rhs_wrapper(n, nu, axes, drag=drag, const_power=cp),
+            A.rhs_vjp_wrapper(n, nu, axes, drag=drag, const_power=cp))
+
+
+CASES = [(3, 32, 5e-3, 0.0, True), (3, 32, 1e-2, 0.05, False), (2, 64, 1e-3, 0.1, False), (2, 64, 2e-3, 0.0, True)]
+
+
+@pytest.mark.parametrize("dim,n,nu,drag,forced", CASES)
+def test_rhs_vjp_matches_oracle(dim, n, nu, drag, forced):
+    from l3es import adjoint as AD
+
+    uh = _state(dim, n, 3)
+    axes, rhs, vjp = _oracle_fns(dim, n, nu, drag, forced)
+    g = _crand(uh.shape, 4, dim, np.abs(uh).max())
+    plan = AD.make_plan(n, nu, dim, 1e-3, "const_power" if forced else "none", kf=2, eps_inj=0.1, drag=drag)
+    got = AD.rhs_vjp(plan, _c64(uh), _c64(g))
+    assert _rel(got, vjp(uh, g)) < 3e-5
+
+
+@pytest.mark.parametrize("dim,n,c", [(3, 64, 16), (3, 32, 32), (2, 64, 32), (2, 32, 8)])
+def test_coarse_mse_matches_oracle(dim, n, c):
+    from l3es import adjoint as AD
+
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    uh = _state(dim, n, 5)
+    tgt = np.random.default_rng(6).standard_normal((dim,) + (c,) * dim).astype(np.float32)
+    ip = AD.coarse_plan(dim, n, c)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    grad = torch.empty(uh.shape, dtype=torch.complex64, device="cuda")
+    ip.coarse_mse(_c64(uh), torch.from_numpy(tgt).cuda(), loss, grad)
+    assert abs(float(loss) - A.coarse_mse(uh, tgt, c, axes)) < 1e-6 * A.coarse_mse(uh, tgt, c, axes)
+    assert _rel(grad, A.coarse_mse_grad(uh, tgt, c, axes)) < 1e-5
+
+
+@pytest.mark.parametrize("dim,n,nu,drag,forced", CASES)
+def test_adjoint_step_matches_oracle(dim, n, nu, drag, forced):
+    from l3es import adjoint as AD
+
+    dt = 2e-3
+    uh = _state(dim, n, 7)
+    axes, rhs, vjp = _oracle_fns(dim, n, nu, drag, forced)
+    lam = _crand(uh.shape, 8, dim)
+    plan = AD.make_plan(n, nu, dim, dt, "const_power" if forced else "none", kf=2, eps_inj=0.1, drag=drag)
+    u0 = _c64(uh)
+    keep = u0.clone()
+    got = _c64(lam)
+    plan.adjoint_step(u0, got)
+    assert torch.equal(u0, keep)  # the checkpoint is not modified
+    assert _rel(got, A.rk4_step_vjp(uh, lam, dt, rhs, vjp)) < 3e-5
+
+
+def test_trajectory_gradient_matches_oracle():
+    from l3es import adjoint as AD
+
+    dim, n, c, nu, dt, steps = 3, 32, 16, 5e-3, 2e-3, 5
+    uh = _state(dim, n, 9)
+    axes, rhs, vjp = _oracle_fns(dim, n, nu, 0.0, True)
+    tgt = 0.5 * np.random.default_rng(10).standard_normal((3, c, c, c)).astype(np.float32)
+    loss_ref, g_ref = A.trajectory_loss_and_grad(uh, steps, dt, rhs, vjp, tgt.astype(np.float64), c, axes)
+    plan = AD.make_plan(n, nu, dim, dt, "const_power", kf=2, eps_inj=0.1)
+    loss, g = AD.loss_and_grad(_c64(uh), plan, steps, torch.from_numpy(tgt).cuda(), AD.coarse_plan(3, n, c))
+    assert abs(float(loss) - loss_ref) < 1e-5 * loss_ref
+    assert _rel(g, g_ref) < 1e-4
+
+
+def test_autograd_matches_direct_sweep():
+    from l3es import adjoint as AD
+
+    n, c, steps = 32, 16, 3
+    uh = _c64(_state(3, n, 11))
+    tgt = torch.from_numpy(np.random.default_rng(12).standard_normal((3, c, c, c)).astype(np.float32)).cuda()
+    plan = AD.make_plan(n, 5e-3, 3, 2e-3, "const_power", kf=2, eps_inj=0.1)
+    ip = AD.coarse_plan(3, n, c)
+    x = uh.clone().requires_grad_(True)
+    loss = AD.coarse_mse(AD.integrate(x, plan, steps), tgt, ip)
+    loss.backward()
+    l2, g2 = AD.loss_and_grad(uh, plan, steps, tgt, ip)
+    assert float(loss.detach()) == float(l2)
+    assert torch.equal(x.grad, g2)
+
+
+def test_ekin_tot_has_no_adjoint():
+    from l3es import _native
+
+    p = _native.Plan(dim=3, n=16, nu=1e-2, dt=1e-3, forcing="ekin_tot", kf=2, e_kin_init=0.5)
+    with pytest.raises(RuntimeError, match="ekin_tot"):
+        p.adjoint_prepare()
+
+
+def _workload128():
+    """128^3 HIT (k_p = 3, constant power 0.1 on |k| <= 2, nu 5e-3), 20 RK4 steps at
+    dt 2e-3, loss = MSE of the 32^3 coarsened velocity against a seeded target
+    (the coarsened HIT field of another seed)."""
+    n, c = 128, 32
+    uh = _state(3, n, 13)
+    tgt = R.spectral_filtering(np.fft.irfftn(_state(3, n, 14), axes=(1, 2, 3)), c)
+    return n, c, 20, 2e-3, uh, np.ascontiguousarray(tgt, dtype=np.float32)
+
+
+def test_differentiation_workload_gradient_vs_fp64():
+    """The FP32 adjoint gradient against the FP64 gradient of the same loss
+    (tests/_fp64_torch.py, the oracle's math in FP64 on the GPU)."""
+    from _fp64_torch import Fp64Model
+
+    from l3es import adjoint as AD
+
+    n, c, steps, dt, uh, tgt = _workload128()
+    plan = AD.make_plan(n, 5e-3, 3, dt, "const_power", kf=2, eps_inj=0.1)
+    loss, g = AD.loss_and_grad(_c64(uh), plan, steps, torch.from_numpy(tgt).cuda(), AD.coarse_plan(3, n, c))
+    M = Fp64Model(n, 5e-3, dt, kf=2, eps_inj=0.1)
+    loss64, g64 = M.loss_and_grad(torch.from_numpy(uh).cuda(), steps, torch.from_numpy(tgt.astype(np.float64)).cuda())
+    assert abs(float(loss) - loss64) < 1e-5 * loss64
+    assert _rel(g, g64.cpu().numpy()) < 1e-4
+
+
+def test_differentiation_workload_finite_differences():
+    """Directional derivatives of the FP32 adjoint gradient against FP64 central
+    differences (step 1e-3) on 16 seeded directions: random HIT fields (k_p = 3
+    spectrum) scaled to the norm of u_hat0. Agreement to 1e-4 of the largest
+    directional derivative."""
+    from _fp64_torch import Fp64Model
+
+    from l3es import adjoint as AD
+
+    n, c, steps, dt, uh, tgt = _workload128()
+    plan = AD.make_plan(n, 5e-3, 3, dt, "const_power", kf=2, eps_inj=0.1)
+    _, g = AD.loss_and_grad(_c64(uh), plan, steps, torch.from_numpy(tgt).cuda(), AD.coarse_plan(3, n, c))
+    g = g.to(torch.complex128)
+    M = Fp64Model(n, 5e-3, dt, kf=2, eps_inj=0.1)
+    u64 = torch.from_numpy(uh).cuda()
+    t64 = torch.from_numpy(tgt.astype(np.float64)).cuda()
+    norm = float(torch.linalg.vector_norm(u64))
+    h = 1e-3
+    ad, fd = [], []
+    for k in range(16):
+        d = torch.from_numpy(_state(3, n, 100 + k)).cuda()
+        d *= norm / float(torch.linalg.vector_norm(d))
+        fd.append((M.loss_after(u64 + h * d, steps, t64) - M.loss_after(u64 - h * d, steps, t64)) / (2 * h))
+        ad.append(float((torch.conj(g) * d).real.sum()))
+    ad, fd = np.array(ad), np.array(fd)
+    assert np.abs(ad - fd).max() < 1e-4 * np.abs(ad).max()
