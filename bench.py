@@ -202,7 +202,8 @@ def run_reference(args):
 # FP64 plain form on the same GPU: the reference algorithm restated with torch.fft
 # (cuFFT) in complex128, op for op (spectral_solver.py:27-120). Comparator only.
 # ---------------------------------------------------------------------------------
-def fp64_plain_rate(u0, dt, n, steps, warmup):
+def fp64_model(n, dt, nu=NU, kf=KF, eps_inj=EPS_INJ):
+    """(rhs, step, weights) of the FP64 plain form at n^3 with constant-power forcing."""
     import torch
 
     dev = "cuda"
@@ -214,7 +215,7 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
     kok2 = kkk / torch.where(kkk2 == 0, torch.ones_like(kkk2), kkk2)
     kmax = 2.0 / 3.0 * (n // 2 + 1)
     dealias = ((kkk.abs() < kmax).all(0)).to(torch.float64)
-    band = ((kkk2 > 0) & (kkk2 <= KF * KF)).to(torch.float64)
+    band = ((kkk2 > 0) & (kkk2 <= kf * kf)).to(torch.float64)
     wts = torch.full((n // 2 + 1,), 2.0, dtype=torch.float64, device=dev)
     wts[0] = wts[-1] = 1.0
     axes = (1, 2, 3)
@@ -225,9 +226,9 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
         du = torch.fft.rfftn(torch.linalg.cross(u, curl, dim=0), dim=axes)
         du = du * dealias
         du = du - (du * kok2).sum(0) * kkk
-        du = du - NU * kkk2 * u_hat
+        du = du - nu * kkk2 * u_hat
         ef = 0.5 * float((wts * ((u_hat * band).abs() ** 2).sum(0)).sum()) / float(n) ** 6
-        return du + (EPS_INJ / (2 * ef + 1e-300)) * u_hat * band
+        return du + (eps_inj / (2 * ef + 1e-300)) * u_hat * band
 
     a = [1 / 6, 1 / 3, 1 / 3, 1 / 6]
     b = [0.5, 0.5, 1.0]
@@ -243,7 +244,14 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
             acc += a[rk] * dt * du
         return acc
 
-    uh = torch.fft.rfftn(torch.from_numpy(u0).to(dev), dim=axes)
+    return rhs, step, wts
+
+
+def fp64_plain_rate(u0, dt, n, steps, warmup):
+    import torch
+
+    _, step, wts = fp64_model(n, dt)
+    uh = torch.fft.rfftn(torch.from_numpy(u0).to("cuda"), dim=(1, 2, 3))
     step(uh.clone())  # creates the cuFFT plans outside the timed region (result discarded)
     for _ in range(warmup):
         uh = step(uh)
@@ -258,6 +266,91 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
     # kinetic energy by Parseval on the half spectrum, FP64
     ke = 0.5 * float((wts * (uh.abs() ** 2).sum(0)).sum()) / float(n) ** 6
     return 1e3 / ms, ke
+
+
+# ---------------------------------------------------------------------------------
+# Differentiation workload: 128^3 HIT (Rogallo k4exp, k_p = 3, KE 0.5, constant power
+# 0.1 on |k| <= 2, nu 5e-3), 20 RK4 steps at dt 2e-3, loss = MSE of the 32^3 spectral
+# coarsening of the final velocity against a seeded target (the coarsened field of
+# another seed). Gradient w.r.t. the initial half spectrum by the hand-written adjoint
+# (per-step checkpoints, stages recomputed). Checks: FP64 central differences (step
+# 1e-3 of a direction with the norm of u_hat0) on seeded random HIT directions, and
+# the FP64 loss. Cost: adjoint step / forward step, CUDA events.
+# ---------------------------------------------------------------------------------
+def adjoint_check(dirs=16, n=128, c=32, steps=20, dt=2e-3, h=1e-3):
+    import torch
+
+    from l3es import adjoint as AD
+    from l3es import init_fields as F
+    from l3es import utils as U
+
+    def hit(seed):
+        u = F.init_u_hit(n, seed, spectrum="k4exp", kp=3.0)
+        return u * np.sqrt(KE0 / (0.5 * np.mean(np.sum(u * u, axis=0))))
+
+    plan = AD.make_plan(n, NU, 3, dt, "const_power", kf=KF, eps_inj=EPS_INJ)
+    ip = AD.coarse_plan(3, n, c)
+
+    def spec(u):
+        out = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
+        plan.rfftn(torch.from_numpy(u.astype(np.float32)).cuda(), out)
+        return out
+
+    uh = spec(hit(SEED))
+    target = U.spectral_filtering(torch.from_numpy(hit(SEED + 1).astype(np.float32)).cuda(), c).float().contiguous()
+    loss, g = AD.loss_and_grad(uh, plan, steps, target, ip)
+    # cost: one forward step vs one adjoint step (warm, CUDA events)
+    x, lam = uh.clone(), g.clone()
+    for _ in range(3):
+        plan.step(x, 1)
+        plan.adjoint_step(uh, lam)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    reps = 20
+    ev[0].record()
+    for _ in range(reps):
+        plan.step(x, 1)
+    ev[1].record()
+    for _ in range(reps):
+        plan.adjoint_step(uh, lam)
+    ev[2].record()
+    torch.cuda.synchronize()
+    fwd_ms, adj_ms = ev[0].elapsed_time(ev[1]) / reps, ev[1].elapsed_time(ev[2]) / reps
+    # FP64 references: the plain form's step and the same coarse MSE in complex128
+    _, step64, _ = fp64_model(n, dt)
+    t64 = target.double()
+
+    def loss64(u_hat):
+        for _ in range(steps):
+            u_hat = step64(u_hat)
+        y = torch.fft.fftshift(torch.fft.fftn(torch.fft.irfftn(u_hat, s=(n, n, n), dim=(1, 2, 3)), dim=(1, 2, 3)),
+                               dim=(1, 2, 3))
+        sl = slice(n // 2 - c // 2, n // 2 + c // 2)
+        y = torch.fft.ifftshift(y[:, sl, sl, sl], dim=(1, 2, 3))
+        uc = (torch.fft.ifftn(y, dim=(1, 2, 3)) / (n / c) ** 3).real
+        return float(((uc - t64) ** 2).mean())
+
+    u64 = uh.to(torch.complex128)
+    l64 = loss64(u64)
+    g64 = g.to(torch.complex128)
+    norm = float(torch.linalg.vector_norm(u64))
+    ad, fd = [], []
+    for k in range(dirs):
+        d = spec(hit(100 + k)).to(torch.complex128)
+        d *= norm / float(torch.linalg.vector_norm(d))
+        fd.append((loss64(u64 + h * d) - loss64(u64 - h * d)) / (2 * h))
+        ad.append(float((torch.conj(g64) * d).real.sum()))
+    ad, fd = np.array(ad), np.array(fd)
+    return {
+        "workload": f"hit3d_{n} k_p=3 const_power, {steps} RK4 steps dt={dt}, loss = MSE of the {c}^3 coarsening vs "
+                    "a seeded target",
+        "fwd_ms_per_step": fwd_ms, "adj_ms_per_step": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+        "target_ratio": 3.0,
+        "loss_fp32": float(loss), "loss_fp64": l64, "loss_rel_err": abs(float(loss) - l64) / l64,
+        "fd": {"directions": dirs, "step": h, "reference": "FP64 plain form (complex128 cuFFT), central differences",
+               "max_abs_err_over_max_abs_dd": float(np.abs(ad - fd).max() / np.abs(ad).max()),
+               "max_rel_err_per_direction": float(np.max(np.abs(ad - fd) / np.abs(fd))), "criterion": 1e-4},
+    }
 
 
 # ---------------------------------------------------------------------------------
@@ -384,6 +477,10 @@ def run_ours(args):
                     "rel_err": abs(ke32 - ke64) / ke64, "criterion": 1e-5}
         del uh_chk
 
+    adjoint = None
+    if rank == 0 and not args.skip_baselines and args.adjoint_dirs > 0:
+        adjoint = adjoint_check(dirs=args.adjoint_dirs)
+
     line = None
     if rank == 0 and args.skip_baselines:
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "ms_per_step": ms, "kernels": kernels,
@@ -409,6 +506,7 @@ def run_ours(args):
             "fp64_plain": {"value": fp64_rate, "unit": "steps/s", "speedup": value / world / fp64_rate,
                            "note": "reference algorithm restated with torch.fft (cuFFT) in complex128, same GPU"},
             "ke_check": ke_check,
+            "adjoint": adjoint,
             "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": "port",
                              "sample": f"1 step at {n}^3 (RK4 + filter + NUFFT + advection), FP64 NumPy/SciPy"},
             "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -586,6 +684,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--ke-steps", type=int, default=200,
                     help="steps of the FP32-vs-FP64 kinetic energy check (0 = skip)")
+    ap.add_argument("--adjoint-dirs", type=int, default=16,
+                    help="directions of the 128^3 adjoint finite-difference check (0 = skip the adjoint leg)")
     ap.add_argument("--skip-baselines", action="store_true",
                     help="profiling runs: time our step only (no FP64 plain, CPU or e2e legs)")
     args = ap.parse_args()
