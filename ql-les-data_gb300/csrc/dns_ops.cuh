@@ -152,7 +152,9 @@ struct DnsOps {
     L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 4.0 * A, s,
                 kx_fwd_plain<N, DIM><<<dim3(xb, 2 * c.batch), TX, 0, s>>>(Y6, c.cs, c.W, c.fs, c.tw));
     const long long pairs = c.cs / 2;
-    L3ES_LAUNCH(c, KK_ADJ_EPI, (a.lam_in ? 7.0 : 6.0) * A + (a.g_out ? A : 0.0), s,
+    // reads: 2 product spectra, g, lam1, lam_in; writes: lam_out, g_out
+    const double epi = (3.0 + (a.lam1 ? 1.0 : 0.0) + (a.lam_in ? 1.0 : 0.0) + 1.0 + (a.g_out ? 1.0 : 0.0)) * A;
+    L3ES_LAUNCH(c, KK_ADJ_EPI, epi, s,
                 k_adj_epi<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(c.W, c.cs, a,
                                                                                                  c.nu_b));
   }
