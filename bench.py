@@ -341,16 +341,38 @@ def adjoint_check(dirs=16, n=128, c=32, steps=20, dt=2e-3, h=1e-3):
         fd.append((loss64(u64 + h * d) - loss64(u64 - h * d)) / (2 * h))
         ad.append(float((torch.conj(g64) * d).real.sum()))
     ad, fd = np.array(ad), np.array(fd)
+    fd_check = None
+    if dirs > 0:
+        fd_check = {"directions": dirs, "step": h,
+                    "reference": "FP64 plain form (complex128 cuFFT), central differences",
+                    "max_abs_err_over_max_abs_dd": float(np.abs(ad - fd).max() / np.abs(ad).max()),
+                    "max_rel_err_per_direction": float(np.max(np.abs(ad - fd) / np.abs(fd))), "criterion": 1e-4}
     return {
         "workload": f"hit3d_{n} k_p=3 const_power, {steps} RK4 steps dt={dt}, loss = MSE of the {c}^3 coarsening vs "
                     "a seeded target",
         "fwd_ms_per_step": fwd_ms, "adj_ms_per_step": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
         "target_ratio": 3.0,
         "loss_fp32": float(loss), "loss_fp64": l64, "loss_rel_err": abs(float(loss) - l64) / l64,
-        "fd": {"directions": dirs, "step": h, "reference": "FP64 plain form (complex128 cuFFT), central differences",
-               "max_abs_err_over_max_abs_dd": float(np.abs(ad - fd).max() / np.abs(ad).max()),
-               "max_rel_err_per_direction": float(np.max(np.abs(ad - fd) / np.abs(fd))), "criterion": 1e-4},
+        "fd": fd_check,
     }
+
+
+def run_adjoint(args):
+    """The differentiation workload alone (one JSON line): time per adjoint step of the
+    128^3, 20-step loss gradient relative to a forward step, and its checks."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    res = adjoint_check(dirs=args.adjoint_dirs)
+    line = {"metric": "adjoint RK4 step cost / forward step at 128^3 (differentiation workload)",
+            "value": res["adjoint_over_forward"], "unit": "ratio", "higher_is_better": False, "n_gpus": 1,
+            "dtype": "f32 (fp64 reductions)", "data": "synthetic", "config": {"workload": res["workload"]},
+            "adjoint": res}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 # ---------------------------------------------------------------------------------
@@ -679,8 +701,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_GRID)
-    ap.add_argument("--workload", default="hit256", choices=["hit256", "batch24"],
-                    help="hit256: the metric's 256^3 step; batch24: 24 mixed trajectories")
+    ap.add_argument("--workload", default="hit256", choices=["hit256", "batch24", "adjoint"],
+                    help="hit256: the metric's 256^3 step; batch24: 24 mixed trajectories; "
+                         "adjoint: the 128^3 differentiation workload alone")
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--ke-steps", type=int, default=200,
                     help="steps of the FP32-vs-FP64 kinetic energy check (0 = skip)")
@@ -693,6 +716,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_batch24(args) if args.workload == "batch24" else run_ours(args)
 
 
