@@ -141,7 +141,7 @@ line_cross_adj(const float2* __restrict__ wm, const float2* __restrict__ wuw, lo
   using C = LineCfg<N>;
   constexpr int M = C::M, H = N / 2 + 1, E = C::E, T = C::T, LPC = C::LPC;
   __shared__ float2 s_x[LPC * C::XS];
-  __shared__ float2 s_m[LPC * 3 * M];
+  __shared__ float2 s_m[LPC * C::PS];
   const int batch = blockIdx.y;
   const int q = threadIdx.x / T, t = threadIdx.x % T;
   const long long line_raw = (long long)blockIdx.x * LPC + q;
@@ -150,7 +150,7 @@ line_cross_adj(const float2* __restrict__ wm, const float2* __restrict__ wuw, lo
   const float2* srcm = wm + (long long)batch * 3 * fs + line * H;
   const float2* srcy = wuw + (long long)batch * 6 * fs + line * H;
   float2* xs = s_x + q * C::XS;
-  float2* sm_ = s_m + q * 3 * M;
+  float2* sm_ = s_m + q * C::PS;
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
     float2 v[E];

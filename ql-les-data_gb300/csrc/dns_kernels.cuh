@@ -40,6 +40,9 @@ struct LineCfg {
   static constexpr int THREADS = 128;
   static constexpr int LPC = LPW * (THREADS / 32);         // lines per CTA
   static constexpr int XS = xpad_len<1>(M);                // exchange slots per line
+  // parked 3-field physical line: stride 3M + T float2, so the 16 / T lines that share a
+  // half warp start T slots apart mod 16 and their 8-byte accesses cover all banks
+  static constexpr int PS = 3 * M + T;
 };
 
 // y-axis pass tiling: radix 16 (one exchange at N = 256) on 16-column tiles where the
@@ -244,7 +247,7 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   using C = LineCfg<N>;
   constexpr int M = C::M, H = N / 2 + 1, E = C::E, T = C::T, LPC = C::LPC;
   __shared__ float2 s_x[LPC * C::XS];
-  __shared__ float2 s_u[LPC * 3 * M];
+  __shared__ float2 s_u[LPC * C::PS];
   const int batch = blockIdx.y;
   const int q = threadIdx.x / T, t = threadIdx.x % T;
   const long long line_raw = (long long)blockIdx.x * LPC + q;
@@ -252,7 +255,7 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   const long long line = valid ? line_raw : nlines - 1;  // idle lines mirror a valid one
   const float2* src = w + (long long)batch * 6 * fs + line * H;
   float2* xs = s_x + q * C::XS;
-  float2* su = s_u + q * 3 * M;
+  float2* su = s_u + q * C::PS;
   float2 cr[3][E];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
