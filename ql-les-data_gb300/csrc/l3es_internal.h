@@ -20,7 +20,6 @@ enum KernelKind {
   KK_LINE_CROSS,    // line_cross
   KK_Y_FWD,         // ky_pass forward (truncated)
   KK_X_EPI,         // kx_fwd_band (band x-FFT + projection)
-  KK_BAND,          // (unused: the band coefficient is computed inside kx_fwd_band)
   KK_FORCE,         // k_force_ekin
   KK_X_INV_PLAIN,   // kx_inv without curl (irfftn)
   KK_LINE_C2R,      // line_c2r

@@ -28,7 +28,7 @@ int cuda_check(cudaError_t e, const char* what) {
 
 const char* kernel_kind_name(int k) {
   static const char* names[KK_COUNT] = {
-      "kx_inv_curl", "ky_pass_inv", "line_cross", "ky_pass_fwd", "kx_fwd_band", "band_scale",
+      "kx_inv_curl", "ky_pass_inv", "line_cross", "ky_pass_fwd", "kx_fwd_band",
       "force_ekin", "kx_inv", "line_c2r", "line_r2c", "kx_fwd", "reduce",
       "filter", "nufft_prep", "nufft_fft", "nufft_gather", "particle_sort", "rk_update",
       "kx_inv_adjproj", "line_cross_adj", "adj_epilogue"};
