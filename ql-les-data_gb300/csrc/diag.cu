@@ -1,5 +1,8 @@
 // Diagnostics of the drivers (l3es/spectral_solver.py:123-127, :318-320;
-// l3es/utils.py:35-97, :300-315) with FP64 accumulation.
+// l3es/utils.py:35-97, :300-315) with FP64 accumulation. Each point's or mode's
+// contribution is formed in FP32 and added to an FP64 sum (one conversion and one
+// FP64 add per element: FP64 arithmetic is scarce on this GPU); the spectral loops run
+// one warp per contiguous half-axis row, so no per-element index division is needed.
 //   l3es_field_stats      max |u_c| per component and 0.5 mean sum u^2 of a physical field
 //   l3es_dissipation      nu <|curl u|^2> by Parseval on the half spectrum
 //   l3es_energy_spectrum  shell sums E(k), shells int(|k| + 0.5)
@@ -19,12 +22,14 @@ k_field_stats(const float* __restrict__ u, long long ps, int nblk, double* __res
   float mx[3] = {0.f, 0.f, 0.f};
   double s = 0.0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ps; i += (long long)nblk * blockDim.x) {
+    float e = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const float v = ub[c * ps + i];
       mx[c] = fmaxf(mx[c], fabsf(v));
-      s += (double)v * v;
+      e = fmaf(v, v, e);
     }
+    s += (double)e;
   }
   __shared__ float smx[3][32];
   __shared__ double ss[32];
@@ -75,7 +80,7 @@ __global__ void k_field_stats_final(const double* __restrict__ partial, int nblk
 // those planes use |(C(k) - conj C(-k)) / 2|^2 with weight 1 (utils.py:312-315).
 template <int DIM>
 __device__ __forceinline__ void curl_at(const float2* __restrict__ ub, long long cs, int n, int kxi, int mid, int kh,
-                                        double* re, double* im) {
+                                        float* re, float* im) {
   const int h = n / 2 + 1;
   const int nmid = DIM == 3 ? n : 1;
   const long long i = ((long long)kxi * nmid + mid) * h + kh;
@@ -83,12 +88,12 @@ __device__ __forceinline__ void curl_at(const float2* __restrict__ ub, long long
   kvec<DIM>(kfull(kxi, n), DIM == 3 ? kfull(mid, n) : 0, kh, k0, k1, k2);
   const float2 a = ub[i], b = ub[cs + i], c = ub[2 * cs + i];
   // (k x u)_x = k1 c - k2 b, (k x u)_y = k2 a - k0 c, (k x u)_z = k0 b - k1 a
-  re[0] = (double)k1 * c.x - (double)k2 * b.x;
-  im[0] = (double)k1 * c.y - (double)k2 * b.y;
-  re[1] = (double)k2 * a.x - (double)k0 * c.x;
-  im[1] = (double)k2 * a.y - (double)k0 * c.y;
-  re[2] = (double)k0 * b.x - (double)k1 * a.x;
-  im[2] = (double)k0 * b.y - (double)k1 * a.y;
+  re[0] = k1 * c.x - k2 * b.x;
+  im[0] = k1 * c.y - k2 * b.y;
+  re[1] = k2 * a.x - k0 * c.x;
+  im[1] = k2 * a.y - k0 * c.y;
+  re[2] = k0 * b.x - k1 * a.x;
+  im[2] = k0 * b.y - k1 * a.y;
 }
 
 template <int DIM>
@@ -98,24 +103,28 @@ k_diss_partial(const float2* __restrict__ uh, long long cs, int n, int nblk, dou
   const float2* ub = uh + (long long)batch * 3 * cs;
   const int h = n / 2 + 1;
   const int nmid = DIM == 3 ? n : 1;
+  const long long rows = cs / h;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double s = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cs; i += (long long)nblk * blockDim.x) {
-    const int kh = (int)(i % h);
-    const long long rest = i / h;
-    const int mid = (int)(rest % nmid);
-    const int kxi = (int)(rest / nmid);
-    double re[3], im[3];
-    curl_at<DIM>(ub, cs, n, kxi, mid, kh, re, im);
-    if (kh == 0 || kh == n / 2) {
-      double re2[3], im2[3];
-      curl_at<DIM>(ub, cs, n, (n - kxi) % n, DIM == 3 ? (n - mid) % n : 0, kh, re2, im2);
-      // Hermitian part of i C is i (C(k) - conj C(-k)) / 2
-      for (int c = 0; c < 3; ++c) {
-        const double hr = 0.5 * (re[c] - re2[c]), hi = 0.5 * (im[c] + im2[c]);
-        s += hr * hr + hi * hi;
+  for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
+    const int mid = (int)(r % nmid), kxi = (int)(r / nmid);
+    for (int kh = lane; kh < h; kh += 32) {
+      float re[3], im[3];
+      curl_at<DIM>(ub, cs, n, kxi, mid, kh, re, im);
+      float e = 0.f;
+      if (kh == 0 || kh == n / 2) {
+        float re2[3], im2[3];
+        curl_at<DIM>(ub, cs, n, (n - kxi) % n, DIM == 3 ? (n - mid) % n : 0, kh, re2, im2);
+        // Hermitian part of i C is i (C(k) - conj C(-k)) / 2
+        for (int c = 0; c < 3; ++c) {
+          const float hr = 0.5f * (re[c] - re2[c]), hi = 0.5f * (im[c] + im2[c]);
+          e = fmaf(hr, hr, fmaf(hi, hi, e));
+        }
+      } else {
+        for (int c = 0; c < 3; ++c) e = fmaf(re[c], re[c], fmaf(im[c], im[c], e));
+        e *= 2.f;
       }
-    } else {
-      for (int c = 0; c < 3; ++c) s += 2.0 * (re[c] * re[c] + im[c] * im[c]);
+      s += (double)e;
     }
   }
   block_sum_store(s, partial, batch * nblk + blockIdx.x);
@@ -133,23 +142,28 @@ k_spectrum(const float2* __restrict__ uh, long long cs, int n, int nblk, double 
   const float2* ub = uh + (long long)batch * 3 * cs;
   const int h = n / 2 + 1;
   const int nmid = DIM == 3 ? n : 1;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cs; i += (long long)nblk * blockDim.x) {
-    const int kh = (int)(i % h);
-    const long long rest = i / h;
-    const int mid = (int)(rest % nmid);
-    const int kx = kfull((int)(rest / nmid), n);
-    const int km = DIM == 3 ? kfull(mid, n) : 0;
-    const double kk = sqrt((double)kx * kx + (double)km * km + (double)kh * kh);
-    const int shell = (int)(kk + 0.5);
-    const double w = (kh == 0 || kh == n / 2) ? 1.0 : 2.0;
-    double e = 0.0;
-    for (int c = 0; c < 3; ++c) {
-      const float2 v = ub[c * cs + i];
-      e += (double)v.x * v.x + (double)v.y * v.y;
-    }
-    if (shell < n) {
-      atomicAdd(&hist[shell], w);
-      atomicAdd(&hist[n + shell], w * e * scale);
+  const long long rows = cs / h;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
+    const int kx = kfull((int)(r / nmid), n);
+    const int km = DIM == 3 ? kfull((int)(r % nmid), n) : 0;
+    const float2* row = ub + r * h;
+    for (int kh = lane; kh < h; kh += 32) {
+      // shell int(|k| + 0.5): |k|^2 is an integer below 3 (n/2)^2, whose square root is
+      // never within 1/(8|k|) of a half integer, far more than the FP32 rounding
+      const int k2 = kx * kx + km * km + kh * kh;
+      const int shell = (int)(sqrtf((float)k2) + 0.5f);
+      float e = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 v = row[c * cs + kh];
+        e = fmaf(v.x, v.x, fmaf(v.y, v.y, e));
+      }
+      if (shell < n) {
+        const double w = (kh == 0 || kh == n / 2) ? 1.0 : 2.0;
+        atomicAdd(&hist[shell], w);
+        atomicAdd(&hist[n + shell], w * scale * (double)e);
+      }
     }
   }
   __syncthreads();
@@ -206,7 +220,7 @@ int l3es_dissipation(l3es_plan* plan, const void* u_hat, double nu, double* out_
   if (!plan || !u_hat || !out_dev) return fail(L3ES_EINVAL, "l3es_dissipation: null argument");
   const Ctx& c = plan_ctx(plan);
   cudaStream_t s = (cudaStream_t)stream;
-  const int nblk = (int)std::min<long long>(608, (c.cs + 255) / 256);
+  const int nblk = (int)std::min<long long>(608, (c.cs / c.h + 7) / 8);  // one warp per row
   const double scale = nu / std::pow((double)c.n, 2 * c.dim);
   if (c.dim == 3)
     L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
@@ -227,7 +241,7 @@ int l3es_energy_spectrum(l3es_plan* plan, const void* u_hat, double mul_fac, dou
   const int n = c.n;
   int rc = cuda_check(cudaMemsetAsync(c.partial, 0, sizeof(double) * 2 * n * c.batch, s), "l3es_energy_spectrum");
   if (rc != L3ES_OK) return rc;
-  const int nblk = (int)std::min<long long>(608, (c.cs + 255) / 256);
+  const int nblk = (int)std::min<long long>(608, (c.cs / c.h + 7) / 8);  // one warp per row
   // |u_hat / n^dim|^2 * mul_fac (utils.py:82-86)
   const double scale = mul_fac / std::pow((double)n, 2 * c.dim);
   const size_t smem = sizeof(double) * 2 * n;

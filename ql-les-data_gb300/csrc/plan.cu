@@ -71,20 +71,29 @@ static std::vector<float2> twiddles(int n) {
 }
 
 // Parseval kinetic energy: per-block partial sums of w |u_hat|^2 over 3 components.
+// One warp per contiguous half-axis row (h modes), so the weight comes from the lane's
+// position and no index division is needed; each mode's energy is formed in FP32 and
+// accumulated in FP64 (one conversion and one FP64 add per mode: FP64 arithmetic is
+// scarce on this GPU).
 __global__ void __launch_bounds__(256)
 k_energy_partial(const float2* __restrict__ uh, long long cs, int h, int nblk, double* __restrict__ partial) {
   const int batch = blockIdx.y;
   const float2* ub = uh + (long long)batch * 3 * cs;
+  const long long rows = cs / h;
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
   double s = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cs; i += (long long)nblk * blockDim.x) {
-    const int kh = (int)(i % h);
-    const double w = (kh == 0 || kh == h - 1) ? 1.0 : 2.0;
-    double a = 0.0;
-    for (int c = 0; c < 3; ++c) {
-      const float2 v = ub[c * cs + i];
-      a += (double)v.x * v.x + (double)v.y * v.y;
+  for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
+    const float2* row = ub + r * h;
+    for (int k = lane; k < h; k += 32) {
+      float e = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 v = row[c * cs + k];
+        e = fmaf(v.x, v.x, e);
+        e = fmaf(v.y, v.y, e);
+      }
+      s += (double)((k == 0 || k == h - 1) ? e : 2.f * e);
     }
-    s += w * a;
   }
   block_sum_store(s, partial, batch * nblk + blockIdx.x);
 }
@@ -344,7 +353,8 @@ int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, voi
   if (!plan || !u_hat || !out_dev) return fail(L3ES_EINVAL, "l3es_kinetic_energy: null argument");
   const Ctx& c = plan->ctx;
   cudaStream_t s = (cudaStream_t)stream;
-  const int nblk = (int)std::min<long long>(c.npartial, (c.cs + 255) / 256);
+  const long long rows = c.cs / c.h;  // one warp per row, 8 per block
+  const int nblk = (int)std::min<long long>(c.npartial, (rows + 7) / 8);
   L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
               k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>((const float2*)u_hat, c.cs, c.h, nblk,
                                                                    c.partial));
