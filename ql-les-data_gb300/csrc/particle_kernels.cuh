@@ -76,7 +76,7 @@ k_crop(const float2* __restrict__ uh, long long cs, int N, float2* __restrict__ 
 // Exact spectral interpolation (interp_backend="dft", integrator.py:62-91):
 // u_r[j] = Re sum_{k in [-c/2, c/2-1]^dim} Hhat(k) exp(i k.x_j) / c^dim.
 // Separable: per (kx[, ky]) an inner sum over the last axis with per-thread phase
-// tables in shared memory (exp(i k x) by sincos in FP64 once per particle and mode).
+// tables in shared memory (exp(i k x) per particle and axis by an FP64 recurrence).
 // ------------------------------------------------------------------------------
 template <int DIM>
 __global__ void __launch_bounds__(128)
@@ -88,11 +88,17 @@ k_dft_interp(const float2* __restrict__ hh, long long hcs, int c, int ncomp, con
   const long long j = valid ? j_raw : 0;
   const int tid = threadIdx.x;
   for (int d = 0; d < DIM; ++d) {
+    // exp(i k x) for k = -c/2 .. c/2-1: two FP64 sincos, then p_{k+1} = p_k exp(i x)
+    // in FP64 (the recurrence adds ~c ulp; FP64 transcendentals are slow on this GPU)
     const double x = r[j * DIM + d];
+    double sn, co, pi, pr;
+    sincos(x, &sn, &co);
+    sincos(-(double)(c / 2) * x, &pi, &pr);
     for (int k = 0; k < c; ++k) {
-      double s, co;
-      sincos((double)(k - c / 2) * x, &s, &co);
-      ph[(d * c + k) * 128 + tid] = make_float2((float)co, (float)s);
+      ph[(d * c + k) * 128 + tid] = make_float2((float)pr, (float)pi);
+      const double tr = pr * co - pi * sn;
+      pi = fma(pr, sn, pi * co);
+      pr = tr;
     }
   }
   const int hc = c / 2 + 1;

@@ -171,21 +171,24 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
   if (i >= np) return;
   const long long j = perm ? perm[i] : i;
   const double two_pi = 2.0 * 3.14159265358979323846;
-  const double h = two_pi / n;
+  const double inv_h = n / two_pi;
   float wk[DIM][W];
   int id[DIM][W];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    const double xs = r[j * DIM + d] / h;
+    // grid coordinate and its offset from the first support point in FP64 (3 FP64
+    // operations per axis; FP64 division is avoided: it is slow on this GPU), the W
+    // kernel arguments z = (t - a) / (W/2) in FP32 as before
+    const double xs = r[j * DIM + d] * inv_h;
     const double l0 = ceil(xs - 0.5 * W);
     const int il0 = (int)l0;
+    const float t = (float)(xs - l0);
 #pragma unroll
     for (int a = 0; a < W; ++a) {
-      const float z = (float)((xs - (l0 + a)) / (0.5 * W));
+      const float z = (t - (float)a) * (2.0f / W);
       const float q = 1.f - z * z;
       wk[d][a] = q > 0.f ? expf(beta * (sqrtf(q) - 1.f)) : 0.f;
-      int g = (il0 + a) % n;
-      id[d][a] = g < 0 ? g + n : g;
+      id[d][a] = (il0 + a) & (n - 1);  // n is a power of two; two's complement wraps negatives
     }
   }
   double ur[3] = {0.0, 0.0, 0.0};
@@ -233,7 +236,7 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
 // Particle -> grid spectrum (turbulence.py:299-339, ur_to_u_dft_wrapper):
 // S_c(k) = sum_j u_r[j][c] exp(-i k . r_j) for every k of the N^dim grid in fftfreq
 // order. One thread per mode; particles streamed through shared memory in tiles of
-// 128 with per-particle 1D phase tables exp(-i k_d x_d) (FP64 sincos, stored FP32);
+// 128 with per-particle 1D phase tables exp(-i k_d x_d) (FP64 recurrence, stored FP32);
 // tile sums in FP32, running total in FP64.
 // ------------------------------------------------------------------------------
 template <int DIM>
@@ -262,11 +265,20 @@ k_p2g_dft(const double* __restrict__ r, const double* __restrict__ u_r, long lon
     if ((int)threadIdx.x < cnt) {
       const long long j = base + threadIdx.x;
       for (int d = 0; d < DIM; ++d) {
+        // exp(-i m x) for m = 0..n/2 by the recurrence p_{m+1} = p_m exp(-i x) in FP64
+        // (one sincos per axis; the recurrence adds ~m ulp), negative k by conjugation
         const double x = r[j * DIM + d];
-        for (int i = 0; i < n; ++i) {
-          double sn, cs;
-          sincos(-(double)kfull(i, n) * x, &sn, &cs);
-          sh[((long long)threadIdx.x * DIM + d) * n + i] = make_float2((float)cs, (float)sn);
+        double sn, cs;
+        sincos(-x, &sn, &cs);
+        double pr = 1.0, pi = 0.0;
+        float2* row = sh + ((long long)threadIdx.x * DIM + d) * n;
+        for (int mm = 0; mm <= n / 2; ++mm) {
+          const float2 v = make_float2((float)pr, (float)pi);
+          if (mm < n / 2) row[mm] = v;
+          if (mm > 0) row[n - mm] = make_float2(v.x, -v.y);
+          const double tr = pr * cs - pi * sn;
+          pi = fma(pr, sn, pi * cs);
+          pr = tr;
         }
       }
       for (int c = 0; c < 3; ++c) su[threadIdx.x][c] = c < ncomp ? (float)u_r[j * ncomp + c] : 0.f;
