@@ -52,7 +52,9 @@ struct DnsOps {
                 kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
                     c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
                     c.eps_inj, c.band));
-    const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 3.0 : rk < 3 ? 5.0 : 3.0);
+    // rk -1: us -> du; 0: us -> out; 1: us, u0 -> acc, out; 2: us, u0, acc -> acc, out;
+    // 3: us, acc -> fin
+    const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);
     const long long pairs = 3 * c.cs / 2;
     L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
                 k_rk_update<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(
