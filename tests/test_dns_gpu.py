@@ -173,3 +173,31 @@ def test_rhs_outside_dealias_band_is_viscous_only(dim, n):
     assert np.abs(d[:, out_x]).max() == 0.0
     ref = R.rhs_wrapper(n, 0.0, axes)(u, uh, 1)
     assert _rel(d, ref) < RTOL
+
+
+def test_step3d_512_vs_fp64():
+    """The largest compiled grid, 512^3: two RK4 steps with constant-power forcing
+    against the FP64 torch restatement of the same step (tests/_fp64_torch.py, equal
+    to the NumPy oracle to 1e-13 on small grids), and the KE reduction against FP64."""
+    from _fp64_torch import Fp64Model
+
+    n, nu, dt = 512, 2e-3, 1e-3
+    u0 = R.init_u_hit(n, 5, spectrum="k4exp", kp=4.0)
+    u0 *= np.sqrt(0.5 / R.kinetic_energy(u0))
+    uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
+    del u0
+    M = Fp64Model(n, nu, dt, kf=2, eps_inj=0.1)
+    ref = torch.from_numpy(uh0).cuda()
+    for _ in range(2):
+        ref = M.step(ref)
+    p = _plan(dim=3, n=n, nu=nu, dt=dt, forcing="const_power", kf=2, eps_inj=0.1)
+    uh = _c64(uh0)
+    del uh0
+    p.step(uh, 2)
+    err = float((uh.to(torch.complex128) - ref).abs().max() / ref.abs().max())
+    assert err < RTOL
+    ke = torch.zeros(1, dtype=torch.float64, device="cuda")
+    p.kinetic_energy(uh, ke)
+    w = M.w
+    ke64 = 0.5 * float((w * (ref.abs() ** 2).sum(0)).sum()) / float(n) ** 6
+    assert abs(float(ke) - ke64) < 1e-6 * ke64
