@@ -114,6 +114,13 @@ const char* l3es_kernel_kind_name(int32_t kind);
 int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
               double* e_inj_dev, void* stream);
 
+/* l3es_step, and the kinetic energy 0.5 <|u|^2> of the final state into ke_dev (device,
+ * batch doubles; the quantity of spectral_solver.py:318), from the same energy pass that
+ * ekin_tot forcing makes anyway (after ekin_tot forcing: the rescaled state's energy),
+ * so it costs at most one pass over u_hat and no separate call or launch sequence. */
+int l3es_step_energy(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
+                     double* e_inj_dev, double* ke_dev, void* stream);
+
 /* rhs_fn(u, u_hat, rk) (l3es/spectral_solver.py:50-60): du = P[dealias *
  * rfftn(u x curl u)] - nu k^2 u_hat (+ enabled extension terms), u from u_hat.
  * du: device, same shape as u_hat, must not alias it. */

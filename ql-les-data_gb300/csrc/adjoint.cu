@@ -110,7 +110,6 @@ int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* str
     prm.kolm_k = d.kolm_k;
     prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
     prm.rk = rk;
-    prm.want_energy = 0;
     plan->tab.stage(c, rk == 0 ? U0 : stage_out[rk - 1], U0, stage_out[rk], rk, prm, s);
   }
   const float dt = (float)d.dt;

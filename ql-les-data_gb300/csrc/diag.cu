@@ -1,8 +1,8 @@
 // Diagnostics of the drivers (l3es/spectral_solver.py:123-127, :318-320;
-// l3es/utils.py:35-97, :300-315) with FP64 accumulation. Each point's or mode's
-// contribution is formed in FP32 and added to an FP64 sum (one conversion and one
-// FP64 add per element: FP64 arithmetic is scarce on this GPU); the spectral loops run
-// one warp per contiguous half-axis row, so no per-element index division is needed.
+// l3es/utils.py:35-97, :300-315) with FP64 partial sums. Each point's or mode's
+// contribution is formed in FP32 and accumulated in float-float (Ff, ~48 bits) or FP64
+// (field statistics); FP64 arithmetic is scarce on this GPU. The spectral loops run one
+// warp per contiguous half-axis row, so no per-element index division is needed.
 //   l3es_field_stats      max |u_c| per component and 0.5 mean sum u^2 of a physical field
 //   l3es_dissipation      nu <|curl u|^2> by Parseval on the half spectrum
 //   l3es_energy_spectrum  shell sums E(k), shells int(|k| + 0.5)
@@ -105,7 +105,7 @@ k_diss_partial(const float2* __restrict__ uh, long long cs, int n, int nblk, dou
   const int nmid = DIM == 3 ? n : 1;
   const long long rows = cs / h;
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  double s = 0.0;
+  Ff s{0.f, 0.f};
   for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
     const int mid = (int)(r % nmid), kxi = (int)(r / nmid);
     for (int kh = lane; kh < h; kh += 32) {
@@ -124,10 +124,10 @@ k_diss_partial(const float2* __restrict__ uh, long long cs, int n, int nblk, dou
         for (int c = 0; c < 3; ++c) e = fmaf(re[c], re[c], fmaf(im[c], im[c], e));
         e *= 2.f;
       }
-      s += (double)e;
+      s = ff_add(s, e);
     }
   }
-  block_sum_store(s, partial, batch * nblk + blockIdx.x);
+  block_sum_store_ff(s, partial, batch * nblk + blockIdx.x);
 }
 
 // energy spectrum: per-block shared-memory histograms of (weight, weight*|u_hat|^2)

@@ -486,8 +486,29 @@ struct EpiParams {
   int kolm_k;        //   (2D extension, kolm_k = 0 = off)
   int band_kf2;      // constant-power band forcing 0 < |k|^2 <= band_kf2 (0 = off)
   int rk;            // 0..3, or -1: write the right-hand side du itself to `out`
-  int want_energy;   // rk == 3: per-CTA partial sums of w |u_hat_new|^2 (FP64 accumulation)
 };
+
+// Float-float (hi + lo) accumulator: error-free FP32 additions (Knuth's TwoSum, then
+// Dekker's fast renormalisation) carry ~48 significant bits without FP64 arithmetic,
+// which is scarce on this GPU. Values are non-negative energies here.
+struct Ff {
+  float hi, lo;
+};
+__device__ __forceinline__ Ff ff_add(Ff a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b - bb);
+  const float lo = a.lo + e;
+  const float h = s + lo;
+  return Ff{h, lo - (h - s)};
+}
+__device__ __forceinline__ Ff ff_add(Ff a, Ff b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+  const float h = s + e;
+  return Ff{h, e - (h - s)};
+}
 
 // FP64 block reduction into partial[block]; all threads must call.
 __device__ __forceinline__ void block_sum_store(double v, double* partial, int block) {
@@ -502,6 +523,27 @@ __device__ __forceinline__ void block_sum_store(double v, double* partial, int b
     v = lane < nw ? red[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) partial[block] = v;
+  }
+}
+
+// Block reduction of float-float partials into partial[block] (FP64): warps combine in
+// float-float by shuffles, the per-warp sums in FP64; all threads must call.
+__device__ __forceinline__ void block_sum_store_ff(Ff v, double* partial, int block) {
+  __shared__ double red_ff[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    Ff w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = ff_add(v, w);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red_ff[wid] = (double)v.hi + (double)v.lo;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) t += red_ff[i];
+    partial[block] = t;
   }
 }
 
@@ -576,7 +618,7 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
 template <int N, int DIM>
 __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a0, float2 z0,
                                           const float2* __restrict__ P, long long pcs, int kt, int kd,
-                                          const EpiParams& prm, float fscale, float2& nv, double& esum) {
+                                          const EpiParams& prm, float fscale, float2& nv) {
   // i < 3 N^2 (N/2+1) < 2^31 for N <= 512: 32-bit division by compile-time constants
   constexpr unsigned H = N / 2 + 1;
   constexpr unsigned NMID = DIM == 3 ? N : 1;
@@ -628,10 +670,6 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
     return make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
   }
   nv = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
-  if (prm.want_energy) {
-    const float wgt = (kh == 0 || kh == N / 2) ? 1.f : 2.f;
-    esum += (double)(wgt * fmaf(nv.x, nv.x, nv.y * nv.y));  // FP32 mode energy, FP64 sum
-  }
   return nv;
 }
 
@@ -639,14 +677,13 @@ template <int N, int DIM>
 __global__ void __launch_bounds__(256)
 k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const float2* us, const float2* u0,
             float2* acc, float2* out, float2* fin, long long cs, EpiParams prm,
-            const double* __restrict__ band_scale, double* __restrict__ partial, const float* __restrict__ nu_b) {
+            const double* __restrict__ band_scale, const float* __restrict__ nu_b) {
   const int batch = blockIdx.y;
   prm.nu = nu_b[batch];  // per-trajectory viscosity
   const long long pairs = 3 * cs / 2;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long bo = (long long)batch * 3 * cs;
   const float fscale = prm.band_kf2 > 0 ? (float)band_scale[batch] : 0.f;
-  double esum = 0.0;
   if (q < pairs) {
     const long long g = 2 * q;  // global element (component-major)
     const float4 s4 = reinterpret_cast<const float4*>(us + bo)[q];
@@ -658,10 +695,10 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
     const unsigned ucs = (unsigned)cs, ug = (unsigned)g;
     const int c0 = (int)(ug / ucs), c1 = (int)((ug + 1u) / ucs);
     const float2 r0 = rk_elem<N, DIM>(ug - (unsigned)c0 * ucs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
-                                      make_float2(z4.x, z4.y), Pb, pcs, kt, kd, prm, fscale, nv0, esum);
+                                      make_float2(z4.x, z4.y), Pb, pcs, kt, kd, prm, fscale, nv0);
     const float2 r1 = rk_elem<N, DIM>(ug + 1u - (unsigned)c1 * ucs, c1, make_float2(s4.z, s4.w),
                                       make_float2(a4.z, a4.w), make_float2(z4.z, z4.w), Pb, pcs, kt, kd, prm,
-                                      fscale, nv1, esum);
+                                      fscale, nv1);
     if (prm.rk < 0) {
       reinterpret_cast<float4*>(out + bo)[q] = make_float4(r0.x, r0.y, r1.x, r1.y);
     } else if (prm.rk < 3) {
@@ -671,11 +708,10 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
       reinterpret_cast<float4*>(fin + bo)[q] = make_float4(nv0.x, nv0.y, nv1.x, nv1.y);
     }
   }
-  if (prm.rk == 3 && prm.want_energy) block_sum_store(esum, partial, batch * gridDim.x + blockIdx.x);
 }
 
 // Lamorgese et al. KE rescaling (spectral_solver.py:82-112), one CTA per trajectory.
-// E_new from the per-CTA partials of kx_fwd_epi (deterministic order), E_low from the
+// E_new from the per-CTA partials of the energy pass (deterministic order), E_low from the
 // band, alpha = sqrt(max(0, (E0 - (E_new - E_low)) / (E_low + eps))), band *= alpha.
 template <int DIM>
 __global__ void __launch_bounds__(256)

@@ -117,7 +117,7 @@ struct Ctx {
   long long fs = 0;     // per field of the 6-field scratch W (== cs)
   long long ds = 0;     // per component of the nonlinear scratch DU (nmid*N*kt)
   long long ps = 0;     // real elements per physical component (N^dim)
-  int npartial = 0;     // CTAs of k_rk_update per trajectory (energy partial sums)
+  int npartial = 0;     // upper bound on the energy pass's CTAs per trajectory
   long long partial_len = 0;  // doubles per trajectory in `partial`
   float2* tw = nullptr;        // N-point twiddle table
   float2* W = nullptr;         // [batch][6][cs]

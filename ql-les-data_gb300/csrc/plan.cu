@@ -73,15 +73,14 @@ static std::vector<float2> twiddles(int n) {
 // Parseval kinetic energy: per-block partial sums of w |u_hat|^2 over 3 components.
 // One warp per contiguous half-axis row (h modes), so the weight comes from the lane's
 // position and no index division is needed; each mode's energy is formed in FP32 and
-// accumulated in FP64 (one conversion and one FP64 add per mode: FP64 arithmetic is
-// scarce on this GPU).
+// accumulated in float-float (Ff), combined across warps and blocks in FP64.
 __global__ void __launch_bounds__(256)
 k_energy_partial(const float2* __restrict__ uh, long long cs, int h, int nblk, double* __restrict__ partial) {
   const int batch = blockIdx.y;
   const float2* ub = uh + (long long)batch * 3 * cs;
   const long long rows = cs / h;
   const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-  double s = 0.0;
+  Ff s{0.f, 0.f};
   for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
     const float2* row = ub + r * h;
     for (int k = lane; k < h; k += 32) {
@@ -92,10 +91,10 @@ k_energy_partial(const float2* __restrict__ uh, long long cs, int h, int nblk, d
         e = fmaf(v.x, v.x, e);
         e = fmaf(v.y, v.y, e);
       }
-      s += (double)((k == 0 || k == h - 1) ? e : 2.f * e);
+      s = ff_add(s, (k == 0 || k == h - 1) ? e : 2.f * e);
     }
   }
-  block_sum_store(s, partial, batch * nblk + blockIdx.x);
+  block_sum_store_ff(s, partial, batch * nblk + blockIdx.x);
 }
 
 __global__ void __launch_bounds__(256)
@@ -276,7 +275,21 @@ int32_t l3es_kernel_kind_count(void) { return KK_COUNT; }
 
 const char* l3es_kernel_kind_name(int32_t kind) { return kernel_kind_name(kind); }
 
-int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, void* stream) {
+}  // extern "C"
+
+// per-block partial sums of w |u_hat|^2 into c.partial ([batch][nblk]); returns nblk
+static int energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {
+  const long long rows = c.cs / c.h;  // one warp per row, 8 per block
+  const int nblk = (int)std::min<long long>(c.npartial, (rows + 7) / 8);
+  L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
+              k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>(uh, c.cs, c.h, nblk, c.partial));
+  return nblk;
+}
+
+// nsteps RK4 steps in place; ke_dev (optional): kinetic energy of the final state per
+// trajectory (for ekin_tot forcing: of the rescaled state)
+static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, double* ke_dev,
+                     void* stream) {
   if (!plan || !u_hat) return fail(L3ES_EINVAL, "l3es_step: null plan or u_hat");
   if (nsteps < 0) return fail(L3ES_EINVAL, "l3es_step: nsteps < 0");
   cudaStream_t s = (cudaStream_t)stream;
@@ -298,25 +311,47 @@ int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double
       prm.kolm_k = d.kolm_k;
       prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
       prm.rk = rk;
-      prm.want_energy = (d.forcing == L3ES_FORCING_EKIN_TOT && rk == 3) ? 1 : 0;
       plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
     }
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
+    double* ke_final = (ke_dev && st == nsteps - 1) ? ke_dev : nullptr;
+    // energy partials of the new state by the row-wise float-float pass (a separate
+    // pass is cheaper than reducing inside the elementwise RK update)
+    int nke = 0;
+    if (d.forcing == L3ES_FORCING_EKIN_TOT || ke_final) nke = energy_partials(c, S, s);
     if (d.forcing == L3ES_FORCING_EKIN_TOT) {
       if (c.dim == 3)
         L3ES_LAUNCH(c, KK_FORCE, 0.0, s,
-                    k_force_ekin<3><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf,
-                                                            inv_n2d, eps64, einj, nullptr));
+                    k_force_ekin<3><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, nke, c.e0, d.dt, c.n, d.kf,
+                                                            inv_n2d, eps64, einj, ke_final));
       else
         L3ES_LAUNCH(c, KK_FORCE, 0.0, s,
-                    k_force_ekin<2><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, c.npartial, c.e0, d.dt, c.n, d.kf,
-                                                            inv_n2d, eps64, einj, nullptr));
-    } else if (e_inj_dev) {
-      L3ES_TRY_CUDA(cudaMemsetAsync(einj, 0, sizeof(double) * c.batch, s), "l3es_step memset");
+                    k_force_ekin<2><<<c.batch, 256, 0, s>>>(S, c.cs, c.partial, nke, c.e0, d.dt, c.n, d.kf,
+                                                            inv_n2d, eps64, einj, ke_final));
+    } else {
+      if (e_inj_dev) L3ES_TRY_CUDA(cudaMemsetAsync(einj, 0, sizeof(double) * c.batch, s), "l3es_step memset");
+      if (ke_final)
+        L3ES_LAUNCH(c, KK_REDUCE, 0.0, s, k_sum_partials<<<c.batch, 256, 0, s>>>(c.partial, nke, 0.5 * inv_n2d, ke_final));
     }
+  }
+  if (nsteps == 0 && ke_dev) {
+    const int rc = l3es_kinetic_energy(plan, u_hat, ke_dev, stream);
+    if (rc != L3ES_OK) return rc;
   }
   if (u_out) plan->tab.irfftn(c, S, u_out, s);
   return cuda_check(cudaGetLastError(), "l3es_step launch");
+}
+
+extern "C" {
+
+int l3es_step(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, void* stream) {
+  return run_steps(plan, u_hat, u_out, nsteps, e_inj_dev, nullptr, stream);
+}
+
+int l3es_step_energy(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, double* ke_dev,
+                     void* stream) {
+  if (!ke_dev) return fail(L3ES_EINVAL, "l3es_step_energy: null ke_dev");
+  return run_steps(plan, u_hat, u_out, nsteps, e_inj_dev, ke_dev, stream);
 }
 
 int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream) {
@@ -332,7 +367,6 @@ int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream) {
   prm.kolm_k = d.kolm_k;
   prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
   prm.rk = -1;
-  prm.want_energy = 0;
   plan->tab.stage(plan->ctx, (const float2*)u_hat, nullptr, (float2*)du, -1, prm, (cudaStream_t)stream);
   return cuda_check(cudaGetLastError(), "l3es_rhs launch");
 }
@@ -353,11 +387,7 @@ int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, voi
   if (!plan || !u_hat || !out_dev) return fail(L3ES_EINVAL, "l3es_kinetic_energy: null argument");
   const Ctx& c = plan->ctx;
   cudaStream_t s = (cudaStream_t)stream;
-  const long long rows = c.cs / c.h;  // one warp per row, 8 per block
-  const int nblk = (int)std::min<long long>(c.npartial, (rows + 7) / 8);
-  L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
-              k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>((const float2*)u_hat, c.cs, c.h, nblk,
-                                                                   c.partial));
+  const int nblk = energy_partials(c, (const float2*)u_hat, s);
   const double scale = 0.5 / std::pow((double)c.n, 2 * c.dim);
   L3ES_LAUNCH(c, KK_REDUCE, 0.0, s, k_sum_partials<<<c.batch, 256, 0, s>>>(c.partial, nblk, scale, out_dev));
   return cuda_check(cudaGetLastError(), "l3es_kinetic_energy launch");

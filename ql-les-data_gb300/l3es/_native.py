@@ -31,6 +31,7 @@ _SIGNATURES = {
     "l3es_graph_launch": (ctypes.c_int, [_P, _P]),
     "l3es_graph_destroy": (ctypes.c_int, [_P]),
     "l3es_step": (ctypes.c_int, [_P, _P, _P, _I, _P, _P]),
+    "l3es_step_energy": (ctypes.c_int, [_P, _P, _P, _I, _P, _P, _P]),
     "l3es_rhs": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_rfftn": (ctypes.c_int, [_P, _P, _P, _P]),
     "l3es_irfftn": (ctypes.c_int, [_P, _P, _P, _P]),
@@ -190,13 +191,23 @@ class Plan:
         vals = (ctypes.c_double * self.batch)(*[float(v) for v in (nu if hasattr(nu, "__len__") else [nu] * self.batch)])
         _check(self._lib.l3es_plan_set_nu(self._h, vals, self.batch), "l3es_plan_set_nu")
 
-    def step(self, u_hat, nsteps: int = 1, u_out=None, e_inj=None, stream=None) -> None:
-        """In-place RK4 steps on u_hat (optionally irfftn into u_out at the end)."""
+    def step(self, u_hat, nsteps: int = 1, u_out=None, e_inj=None, ke=None, stream=None) -> None:
+        """In-place RK4 steps on u_hat (optionally irfftn into u_out at the end). ke: a
+        float64 device tensor of `batch` values that receives the kinetic energy of the
+        final state (taken from the last stage's energy sums, no extra pass)."""
         self._check_spec(u_hat)
         if u_out is not None:
             self._check_phys(u_out)
-        _check(self._lib.l3es_step(self._h, _ptr(u_hat), _ptr(u_out), int(nsteps), _ptr(e_inj),
-                                   _stream(stream)), "l3es_step")
+        if ke is None:
+            _check(self._lib.l3es_step(self._h, _ptr(u_hat), _ptr(u_out), int(nsteps), _ptr(e_inj),
+                                       _stream(stream)), "l3es_step")
+            return
+        import torch
+
+        if ke.dtype != torch.float64 or ke.numel() < self.batch:
+            raise ValueError("ke must hold `batch` float64 values")
+        _check(self._lib.l3es_step_energy(self._h, _ptr(u_hat), _ptr(u_out), int(nsteps), _ptr(e_inj), _ptr(ke),
+                                          _stream(stream)), "l3es_step_energy")
 
     def rhs(self, u_hat, du, stream=None) -> None:
         self._check_spec(u_hat)

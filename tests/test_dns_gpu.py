@@ -201,3 +201,25 @@ def test_step3d_512_vs_fp64():
     w = M.w
     ke64 = 0.5 * float((w * (ref.abs() ** 2).sum(0)).sum()) / float(n) ** 6
     assert abs(float(ke) - ke64) < 1e-6 * ke64
+
+
+@pytest.mark.parametrize("forcing", ["none", "const_power", "ekin_tot"])
+def test_step_energy_equals_kinetic_energy(forcing):
+    """l3es_step_energy's KE (after ekin_tot rescaling: e_high + alpha^2 e_low) equals
+    l3es_kinetic_energy of the final state; batch of 2."""
+    n = 32
+    us = []
+    for b in range(2):
+        u = R.init_u_hit(n, 40 + b, spectrum="k4exp", kp=3.0)
+        us.append(np.fft.rfftn(u * np.sqrt(0.5 / R.kinetic_energy(u)), axes=(1, 2, 3)))
+    p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3, batch=2, forcing=forcing, kf=2, eps_inj=0.1, e_kin_init=0.5)
+    uh = torch.stack([_c64(x) for x in us]).contiguous()
+    ke = torch.zeros(2, dtype=torch.float64, device="cuda")
+    p.step(uh, 3, ke=ke)
+    ref = torch.zeros(2, dtype=torch.float64, device="cuda")
+    p.kinetic_energy(uh, ref)
+    # ekin_tot reports e_high + alpha^2 e_low of the rescaling, the recount sees the
+    # rescaled FP32 state; otherwise only the FP32 rounding of the mode energies differs
+    np.testing.assert_allclose(ke.cpu().numpy(), ref.cpu().numpy(), rtol=1e-6 if forcing == "ekin_tot" else 1e-7)
+    if forcing == "ekin_tot":
+        np.testing.assert_allclose(ke.cpu().numpy(), 0.5, rtol=1e-6)
