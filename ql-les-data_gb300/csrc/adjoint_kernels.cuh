@@ -155,7 +155,7 @@ line_cross_adj(const float2* __restrict__ wm, const float2* __restrict__ wuw, lo
   for (int f = 0; f < 3; ++f) {
     float2 v[E];
     c2r_load_pack<M, E>(srcm + f * fs, t, v, twN, scale);
-    warp_fft<M, E, kInv>(v, xs, t, twN, 2);
+    warp_fft<M, E, kInv>(v, xs, t, twN + N);
 #pragma unroll
     for (int e = 0; e < E; ++e) sm_[f * M + t + T * e] = v[e];  // physical values at 2n, 2n+1
     __syncwarp();
@@ -172,7 +172,7 @@ line_cross_adj(const float2* __restrict__ wm, const float2* __restrict__ wuw, lo
     for (int f = 0; f < 3; ++f) {
       float2 v[E];
       c2r_load_pack<M, E>(srcy + (3 * grp + f) * fs, t, v, twN, scale);
-      warp_fft<M, E, kInv>(v, xs, t, twN, 2);
+      warp_fft<M, E, kInv>(v, xs, t, twN + N);
 #pragma unroll
       for (int e = 0; e < E; ++e) {
         const int n = t + T * e;
@@ -201,7 +201,7 @@ line_cross_adj(const float2* __restrict__ wm, const float2* __restrict__ wuw, lo
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      warp_fft<M, E, kFwd>(cr[c], xs, t, twN, 2);
+      warp_fft<M, E, kFwd>(cr[c], xs, t, twN + N);
       float2 X[E];
       r2c_unpack_regs<M, E>(cr[c], t, twN, X);
       if (valid) {

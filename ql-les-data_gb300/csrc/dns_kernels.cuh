@@ -171,18 +171,14 @@ __device__ __forceinline__ float2 c2r_pack_pair(float2 a, float2 b, int k, const
   return make_float2(scale * (s.x + id.x), scale * (s.y + id.y));
 }
 
-// Loads one half-spectrum line for an M-point c2r by T = M/E threads of one warp
-// (thread t holds k = t + T e) and packs it. X[k] is read once per element: the
-// partner X[M-k] lives in thread (T - t) mod T, slot E-1-e (slot (E-e) mod E for
-// t = 0, plus X[M] for k = 0), and arrives by warp shuffle.
+// Packs one half-spectrum line for an M-point c2r by T = M/E threads of one warp
+// (thread t holds xk[e] = X[t + T e]; xm = X[M] is used by t = 0 only). Each X[k] is
+// read once: the partner X[M-k] lives in thread (T - t) mod T, slot E-1-e (slot
+// (E-e) mod E for t = 0, plus X[M] for k = 0), and arrives by warp shuffle.
 template <int M, int E>
-__device__ __forceinline__ void c2r_load_pack(const float2* __restrict__ X, int t, float2 (&v)[E],
-                                              const float2* __restrict__ twN, float scale) {
+__device__ __forceinline__ void c2r_pack(const float2 (&xk)[E], float2 xm, int t, float2 (&v)[E],
+                                         const float2* __restrict__ twN, float scale) {
   constexpr int T = M / E;
-  float2 xk[E];
-#pragma unroll
-  for (int e = 0; e < E; ++e) xk[e] = __ldg(X + t + T * e);
-  const float2 xm = __ldg(X + M);  // Nyquist, used by t = 0
   const int lane = threadIdx.x & 31;
   const int src = lane - t + (t == 0 ? 0 : T - t);
 #pragma unroll
@@ -194,6 +190,18 @@ __device__ __forceinline__ void c2r_load_pack(const float2* __restrict__ X, int 
     if (t == 0 && e == 0) b = xm;
     v[e] = c2r_pack_pair(xk[e], b, t + T * e, twN, scale);
   }
+}
+
+// c2r_pack of a line read from global memory
+template <int M, int E>
+__device__ __forceinline__ void c2r_load_pack(const float2* __restrict__ X, int t, float2 (&v)[E],
+                                              const float2* __restrict__ twN, float scale) {
+  constexpr int T = M / E;
+  float2 xk[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) xk[e] = __ldg(X + t + T * e);
+  const float2 xm = __ldg(X + M);  // Nyquist, used by t = 0
+  c2r_pack<M, E>(xk, xm, t, v, twN, scale);
 }
 
 // M-point forward FFT output Z (exchange buffer, padded index) -> r2c value X[k],
@@ -269,7 +277,7 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   for (int f = 0; f < 6; ++f) {
     float2 v[E];
     c2r_load_pack<M, E>(src + f * fs, t, v, twN, scale);
-    warp_fft<M, E, kInv>(v, xs, t, twN, 2);
+    warp_fft<M, E, kInv>(v, xs, t, twN + N);
     // v[e] packs the physical values at 2n and 2n+1, n = t + T*e
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -302,7 +310,7 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
   float2* db = du + (long long)batch * 3 * ds + line * kt;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    warp_fft<M, E, kFwd>(cr[c], xs, t, twN, 2);
+    warp_fft<M, E, kFwd>(cr[c], xs, t, twN + N);
     float2 X[E];
     r2c_unpack_regs<M, E>(cr[c], t, twN, X);
     if (valid) {
@@ -339,7 +347,7 @@ line_c2r(const float2* __restrict__ w, long long fs, float* __restrict__ out, lo
     const float2* src = w + (long long)batch * 3 * fs + f * fs + line * H;
     float2 v[E];
     c2r_load_pack<M, E>(src, t, v, twN, scale);
-    warp_fft<M, E, kInv>(v, xs, t, twN, 2);
+    warp_fft<M, E, kInv>(v, xs, t, twN + N);
     if (valid) {
       float2* dst = reinterpret_cast<float2*>(out + (long long)batch * 3 * os + f * os + line * N);
 #pragma unroll
@@ -371,7 +379,7 @@ line_r2c(const float* __restrict__ in, long long is, float2* __restrict__ w, lon
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = __ldg(src + t + T * e);
-    warp_fft<M, E, kFwd>(v, xs, t, twN, 2);
+    warp_fft<M, E, kFwd>(v, xs, t, twN + N);
     float2 X[E];
     r2c_unpack_regs<M, E>(v, t, twN, X);
     if (valid) {

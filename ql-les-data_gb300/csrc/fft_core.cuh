@@ -8,7 +8,10 @@
 // so a forward FFT can consume the register output of an inverse FFT directly.
 //
 // Twiddles come from a table tw[m] = exp(-2 pi i m / Ntab) computed in FP64 on the
-// host and stored FP32; an N-point FFT indexes it with stride Ntab / N.
+// host and stored FP32; an N-point FFT indexes it with stride Ntab / N. FFTs whose
+// threads sit in one warp can instead read a compact per-stage table (CT = true, see
+// Sched::ctoff) in which the twiddles of one stage are contiguous in the thread index,
+// so a warp's twiddle load touches one or two 128-byte lines instead of up to eight.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -132,6 +135,11 @@ struct Sched {
   static constexpr int kStages = kFull + (kRem > 1 ? 1 : 0);
   static constexpr int radix(int s) { return s < kFull ? E : kRem; }
   static constexpr int ns(int s) { return ipow(E, s); }  // Ns before stage s
+  // compact twiddle table: stage s >= 1 holds (radix(s) - 1) x ns(s) entries
+  // ct[ctoff(s) + (r - 1) ns(s) + jm] = exp(-2 pi i r jm / (ns(s) radix(s))), r >= 1,
+  // jm < ns(s); stage 0 (Ns = 1) needs none
+  static constexpr int ctoff(int s) { return s <= 1 ? 0 : ctoff(s - 1) + (radix(s - 1) - 1) * ns(s - 1); }
+  static constexpr int ctlen() { return ctoff(kStages); }
 };
 
 // Exchange index per layout, chosen with a shared-memory bank model (8-byte
@@ -158,7 +166,8 @@ __device__ __forceinline__ void fft_sync() {
 // One Stockham stage. FIRST: inputs from registers; LAST: outputs to registers.
 // sm: exchange buffer, element n at sm[xpad<SS>(n) * SS]. WARP: all T threads of the
 // FFT are in one warp, so __syncwarp orders the exchanges.
-template <int N, int E, int R, int NS, int DIR, int SS, bool WARP, bool FIRST, bool LAST>
+// CT: tw is the compact table at this stage's offset (tws unused).
+template <int N, int E, int R, int NS, int DIR, int SS, bool WARP, bool FIRST, bool LAST, bool CT = false>
 __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t,
                                                const float2* __restrict__ tw, int tws) {
   constexpr int T = N / E;
@@ -179,7 +188,8 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
     if (NS > 1) {
       const int jm = j % NS;
 #pragma unroll
-      for (int r = 1; r < R; ++r) x[b][r] = cmul(x[b][r], twid<DIR>(tw, r * jm * (N / (NS * R)) * tws));
+      for (int r = 1; r < R; ++r)
+        x[b][r] = cmul(x[b][r], twid<DIR>(tw, CT ? (r - 1) * NS + jm : r * jm * (N / (NS * R)) * tws));
     }
     Dft<R, DIR>::run(x[b]);
     if (LAST) {
@@ -194,51 +204,51 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], float2* sm, int t
   if (!LAST) fft_sync<WARP>();
 }
 
-template <int N, int E, int DIR, int SS, bool WARP, int S, bool DONE = (S >= Sched<N, E>::kStages)>
+template <int N, int E, int DIR, int SS, bool WARP, bool CT, int S, bool DONE = (S >= Sched<N, E>::kStages)>
 struct Stages;
-template <int N, int E, int DIR, int SS, bool WARP, int S>
-struct Stages<N, E, DIR, SS, WARP, S, false> {
+template <int N, int E, int DIR, int SS, bool WARP, bool CT, int S>
+struct Stages<N, E, DIR, SS, WARP, CT, S, false> {
   using Sc = Sched<N, E>;
   static __device__ __forceinline__ void run(float2 (&v)[E], float2* sm, int t,
                                              const float2* __restrict__ tw, int tws) {
-    stockham_stage<N, E, Sc::radix(S), Sc::ns(S), DIR, SS, WARP, S == 0, S == Sc::kStages - 1>(v, sm, t, tw,
-                                                                                               tws);
-    Stages<N, E, DIR, SS, WARP, S + 1>::run(v, sm, t, tw, tws);
+    stockham_stage<N, E, Sc::radix(S), Sc::ns(S), DIR, SS, WARP, S == 0, S == Sc::kStages - 1, CT>(
+        v, sm, t, CT ? tw + Sc::ctoff(S) : tw, tws);
+    Stages<N, E, DIR, SS, WARP, CT, S + 1>::run(v, sm, t, tw, tws);
   }
 };
-template <int N, int E, int DIR, int SS, bool WARP, int S>
-struct Stages<N, E, DIR, SS, WARP, S, true> {
+template <int N, int E, int DIR, int SS, bool WARP, bool CT, int S>
+struct Stages<N, E, DIR, SS, WARP, CT, S, true> {
   static __device__ __forceinline__ void run(float2 (&)[E], float2*, int, const float2* __restrict__, int) {}
 };
 
 // N-point FFT by T = N/E threads; every thread of the CTA (WARP = false) or of the
 // warp (WARP = true) must call it, since it synchronises between stages. v[e] holds
 // element t + T*e on entry and on exit. tws: stride into the twiddle table (table
-// length / N). The exchange buffer is free on return only after the caller's next
+// length / N); with CT, tw is the compact table of the N-point FFT instead. The exchange buffer is free on return only after the caller's next
 // barrier of the same scope.
-template <int N, int E, int DIR, int SS, bool WARP = false>
+template <int N, int E, int DIR, int SS, bool WARP = false, bool CT = false>
 __device__ __forceinline__ void block_fft(float2 (&v)[E], float2* sm, int t,
                                           const float2* __restrict__ tw, int tws) {
-  Stages<N, E, DIR, SS, WARP, 0>::run(v, sm, t, tw, tws);
+  Stages<N, E, DIR, SS, WARP, CT, 0>::run(v, sm, t, tw, tws);
 }
 
 // N-point FFT whose T = N/E threads sit in one warp (per-line buffers, SS = 1). For
 // N = 2 E^2 (e.g. 128 = 8 x 8 x 2) the final radix-2 stage pairs element j with
 // j + N/2; after the second stage they sit in the same register slot of lanes t and
 // t ^ E, so that stage exchanges by warp shuffle instead of a shared-memory round
-// trip. Other sizes use the shared-memory Stockham schedule.
+// trip. Other sizes use the shared-memory Stockham schedule. ct: the compact twiddle
+// table of the N-point FFT (Sched<N, E>::ctoff layout, length Sched<N, E>::ctlen()).
 template <int N, int E, int DIR>
-__device__ __forceinline__ void warp_fft(float2 (&v)[E], float2* sm, int t, const float2* __restrict__ tw,
-                                         int tws) {
+__device__ __forceinline__ void warp_fft(float2 (&v)[E], float2* sm, int t, const float2* __restrict__ ct) {
   using Sc = Sched<N, E>;
   constexpr bool kTail2 = Sc::kStages == 3 && Sc::radix(0) == E && Sc::radix(1) == E && Sc::radix(2) == 2 &&
                           N / E == 2 * E && N / E <= 32;
   if constexpr (!kTail2) {
-    block_fft<N, E, DIR, 1, true>(v, sm, t, tw, tws);
+    block_fft<N, E, DIR, 1, true, true>(v, sm, t, ct, 0);
   } else {
     constexpr int T = N / E;
     // stage 0: radix E on the registers, out to shared memory
-    stockham_stage<N, E, E, 1, DIR, 1, true, true, false>(v, sm, t, tw, tws);
+    stockham_stage<N, E, E, 1, DIR, 1, true, true, false>(v, sm, t, ct, 0);
     // stage 1: radix E (Ns = E), one butterfly per thread, outputs stay in registers:
     // slot r holds element (t / E) N/2 + t % E + r E
     {
@@ -247,7 +257,7 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[E], float2* sm, int t, cons
       for (int r = 0; r < E; ++r) x[r] = sm[xpad<1, E>(t + r * (N / E))];
       const int jm = t % E;
 #pragma unroll
-      for (int r = 1; r < E; ++r) x[r] = cmul(x[r], twid<DIR>(tw, r * jm * (N / (E * E)) * tws));
+      for (int r = 1; r < E; ++r) x[r] = cmul(x[r], twid<DIR>(ct, Sc::ctoff(1) + (r - 1) * E + jm));
       Dft<E, DIR>::run(x);
 #pragma unroll
       for (int r = 0; r < E; ++r) v[r] = x[r];
@@ -266,7 +276,7 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[E], float2* sm, int t, cons
         const float2 a = hi ? got : v[2 * b];
         float2 c = hi ? v[2 * b + 1] : got;
         const int j = t + T * b;
-        c = cmul(c, twid<DIR>(tw, j * tws));
+        c = cmul(c, twid<DIR>(ct, Sc::ctoff(2) + j));
         y[b] = cadd(a, c);
         y[b + E / 2] = csub(a, c);
       }

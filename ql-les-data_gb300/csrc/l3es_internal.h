@@ -119,7 +119,7 @@ struct Ctx {
   long long ps = 0;     // real elements per physical component (N^dim)
   int npartial = 0;     // upper bound on the energy pass's CTAs per trajectory
   long long partial_len = 0;  // doubles per trajectory in `partial`
-  float2* tw = nullptr;        // N-point twiddle table
+  float2* tw = nullptr;        // N-point twiddle table + compact table of the N/2-point line FFT
   float2* W = nullptr;         // [batch][6][cs]
   float2* DU = nullptr;        // [batch][3][ds]
   float2* Tb = nullptr;        // [batch][3][cs] RK stage field

@@ -59,13 +59,35 @@ static int dealias_kd(int n) {
   return kd;
 }
 
-// FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n)
+static float2 twiddle(long long m, long long n) {
+  const double pi = 3.14159265358979323846;
+  const double a = -2.0 * pi * (double)m / (double)n;
+  return make_float2((float)std::cos(a), (float)std::sin(a));
+}
+
+// FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n), followed by the compact
+// per-stage table of the n/2-point line FFT (radix-8 schedule; Sched::ctoff layout):
+// for stage s >= 1 of radix R with Ns points per sub-transform, entries r = 1..R-1,
+// jm = 0..Ns-1 hold exp(-2 pi i r jm / (Ns R)). Same FP64 angles (scaled by powers of
+// two) as the strided table, so both give the same FP32 values.
 static std::vector<float2> twiddles(int n) {
   std::vector<float2> t(n);
-  const double pi = 3.14159265358979323846;
-  for (int m = 0; m < n; ++m) {
-    const double a = -2.0 * pi * (double)m / (double)n;
-    t[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  for (int m = 0; m < n; ++m) t[m] = twiddle(m, n);
+  const int M = n / 2, E = M >= 8 ? 8 : M;
+  std::vector<int> radix;
+  int rem = M;
+  while (E > 1 && rem >= E) {
+    radix.push_back(E);
+    rem /= E;
+  }
+  if (rem > 1) radix.push_back(rem);
+  long long ns = 1;
+  for (size_t st = 0; st < radix.size(); ++st) {
+    const int R = radix[st];
+    if (st >= 1)
+      for (int r = 1; r < R; ++r)
+        for (long long jm = 0; jm < ns; ++jm) t.push_back(twiddle(r * jm, ns * R));
+    ns *= R;
   }
   return t;
 }
@@ -191,7 +213,8 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
 
   const size_t B = (size_t)c.batch;
   int rc = L3ES_OK;
-  rc = rc ? rc : plan_alloc(p, (void**)&c.tw, sizeof(float2) * n, "twiddles");
+  const std::vector<float2> tw = twiddles(n);
+  rc = rc ? rc : plan_alloc(p, (void**)&c.tw, sizeof(float2) * tw.size(), "twiddles");
   rc = rc ? rc : plan_alloc(p, (void**)&c.W, sizeof(float2) * B * 6 * c.fs, "W");
   rc = rc ? rc : plan_alloc(p, (void**)&c.DU, sizeof(float2) * B * 3 * c.ds, "DU");
   rc = rc ? rc : plan_alloc(p, (void**)&c.Tb, sizeof(float2) * B * 3 * c.cs, "stage");
@@ -207,10 +230,9 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
     delete p;
     return rc;
   }
-  std::vector<float2> tw = twiddles(n);
   std::vector<double> e0(B, desc->e_kin_init);
   std::vector<float> nus(B, (float)desc->nu);
-  cudaError_t e = cudaMemcpy(c.tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(c.tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c.nu_b, nus.data(), sizeof(float) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
