@@ -333,6 +333,39 @@ def init_u_random2d(N, seed=0, kmax=8.0, energy=0.5, target_dim=3):
 # ---------------------------------------------------------------------------------
 # solver set-up (l3es/spectral_solver.py:156-230)
 # ---------------------------------------------------------------------------------
+def init_u_kolm(N, L=2 * np.pi, max_velocity=4.2, seed=42, target_dim=3, iter=4,
+                grid_n=2048, peak_wavenumber=4.0):
+    """Kolmogorov initial field (init_fields.py:191-212), restating JAX-CFD's
+    filtered_velocity_field on a grid_n^2 grid of side L: seeded white noise
+    (np.random.default_rng(seed), 2 components), radial log-normal filter
+    exp(-(ln k - ln k_p)^2 / 2) / k with k in cycles per unit length (Nyquist row and
+    column zeroed), then `iter` x (Leray projection, scale max |u| to max_velocity),
+    then spectral_filtering to N^2. Full complex FFTs here. PARITY UNPINNED: JAX's
+    generator and JAX-CFD are unavailable, so this only checks the drop-in's own
+    restatement of the same construction."""
+    G = grid_n
+    rng = np.random.default_rng(seed)
+    noise = rng.standard_normal((2, G, G))
+    k1 = np.fft.fftfreq(G, L / G)
+    KX, KY = np.meshgrid(k1, k1, indexing="ij")
+    kk = np.hypot(KX, KY)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        filt = np.where(kk > 0, np.exp(-0.5 * (np.log(kk) - np.log(peak_wavenumber)) ** 2) / kk, 0.0)
+    filt[G // 2, :] = 0.0
+    filt[:, G // 2] = 0.0
+    vh = _fftn(noise, axes=(1, 2)) * filt
+    k2 = np.where(kk > 0, kk * kk, 1.0)
+    for _ in range(max(1, iter)):
+        kv = (KX * vh[0] + KY * vh[1]) / k2
+        vh = np.array([vh[0] - KX * kv, vh[1] - KY * kv])
+        v = _ifftn(vh, axes=(1, 2)).real
+        vh = vh * (max_velocity / np.max(np.sqrt(np.sum(v * v, axis=0))))
+    u = spectral_filtering(_ifftn(vh, axes=(1, 2)).real, N)[..., None]
+    if target_dim == 3:
+        u = np.concatenate([u, np.zeros((1, N, N, 1))], axis=0)
+    return u
+
+
 def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None,
                   forcing_type="ekin_tot", warmup=True, **ext):
     """Host restatement of spectral_solver.py:156-230 (no executable cache).
@@ -354,9 +387,11 @@ def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None,
         u = init_u_tgv2d(N, target_dim=3, rescale=L)
     elif case == "HIT":
         u = init_u_hit(N, seed, ext.get("spectrum", "k-5/3"), ext.get("kp", 4.0))
-    elif case == "Kolm":
+    elif case == "Kolm" and ext.get("init", "kolm") == "random2d":
         u = init_u_random2d(N, seed, ext.get("init_kmax", 8.0),
                             ext.get("init_energy", 0.5))
+    elif case == "Kolm":
+        u = init_u_kolm(N, seed=seed, target_dim=3, grid_n=ext.get("kolm_grid", 2048))
     else:
         raise ValueError(case)
     e_kin_init = 0.5 * np.mean(np.sum(u * u, axis=0))

@@ -13,12 +13,13 @@ which also advects the particles with the relaxed velocity). The SPH density max
 is logged on log/checkpoint steps as in the reference. Outside this package: plots.
 Particle checkpoints go to step_XXXXX.npz files with the reference's keys r and u (the
 unrelaxed interpolated velocity, as the reference writes; the reference writes h5
-through JAX-SPH).
+through JAX-SPH), and the run's settings to config.json (sim / com sections).
 """
 
 from __future__ import annotations
 
 import csv
+import json
 import os
 from time import time
 
@@ -40,6 +41,16 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
     dst_path = dst_path or "results"
     int_path = os.path.join(dst_path, "com")
     os.makedirs(int_path, exist_ok=True)
+    # the run's settings in the reference's config layout (main.py:72-73 saves the merged
+    # config.yaml beside the trajectory); gen_dataset reads it for the dataset metadata
+    with open(os.path.join(dst_path, "config.json"), "w") as f:
+        json.dump({"mode": "combined", "seed": seed,
+                   "sim": {"case": case, "N": N, "dim": dim, "nu": nu, "t_final": t_final, "t_burnin": t_burnin,
+                           "dt": dt, "u_ref": u_ref, "ckp_N": ckp_N, "forcing_type": forcing_type,
+                           "e_kin_target": e_kin_target, "kf": kf},
+                   "com": {"state_0_path": state_0_path, "interp_backend": interp_backend,
+                           "relax_dt_factor": relax_dt_factor, "dft_splits": dft_splits, "log_freq": log_freq,
+                           "vis_freq": vis_freq, "ckp_freq": ckp_freq, "dst_path": dst_path}}, f, indent=1)
     diagnostics_path = os.path.join(dst_path, "diagnostics.csv")
     with open(diagnostics_path, "w", newline="") as f:
         csv.writer(f).writerow(["step", "time", "umax", "ekin", "dt_est", "e_inj", "rho_max"])

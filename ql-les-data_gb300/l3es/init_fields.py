@@ -128,3 +128,67 @@ def init_u_random2d(N, seed=0, kmax=8.0, energy=0.5, target_dim=3):
     if target_dim == 3:
         uv = np.concatenate([uv[..., None], np.zeros((1, N, N, 1))], axis=0)
     return uv
+
+
+def _spectral_filter_np(u, c):
+    """spectral_filtering (utils.py:100-138) of (ncomp, G, G) in FP64: full FFT, keep the
+    shifted modes [G/2 - c/2, G/2 + c/2) of each axis (k in [-c/2, c/2-1]), inverse FFT
+    on the c grid divided by (G/c)^2, real part."""
+    G = u.shape[-1]
+    uh = np.fft.fftshift(np.fft.fftn(u, axes=(1, 2)), axes=(1, 2))
+    sl = slice(G // 2 - c // 2, G // 2 + c // 2)
+    uh = np.fft.ifftshift(uh[:, sl, sl], axes=(1, 2))
+    return np.fft.ifftn(uh, axes=(1, 2)).real / (G / c) ** 2
+
+
+def _lognormal_density(k, peak):
+    """Log-normal radial spectral filter exp(-(ln k - ln peak)^2 / 2) / k (the 1/k spreads
+    the 2D shell area so the shell energy, not the mode amplitude, is log-normal); 0 at k=0."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        d = np.exp(-0.5 * (np.log(k) - np.log(peak)) ** 2) / k
+    return np.where(k > 0, d, 0.0)
+
+
+def init_u_kolm(N, L=2 * np.pi, max_velocity=4.2, seed=42, target_dim=3, iter=4, grid_n=2048,
+                peak_wavenumber=4.0):
+    """Kolmogorov-flow initial field (drop-in for init_fields.py:191-212).
+
+    The reference builds it with JAX-CFD's filtered_velocity_field on a 2048^2 grid of
+    side L and coarsens it to N x N with spectral_filtering. Restated here in FP64 NumPy
+    (JAX-CFD and JAX's random generator are not available, so values are seeded by
+    ``np.random.default_rng(seed)`` instead and do not match the reference bit for bit):
+      1. white Gaussian noise for each of the 2 velocity components on grid_n^2 points;
+      2. radial spectral filter with a log-normal density peaked at `peak_wavenumber`
+         (wavenumbers in cycles per unit length, the grid's fftfreq(grid_n, L/grid_n));
+      3. `iter` times: divergence-free (Leray) projection, then scaling so that the
+         largest pointwise speed equals `max_velocity`;
+      4. keep the modes k in [-N/2, N/2-1] of each axis and transform back on the N^2
+         grid, i.e. spectral_filtering (utils.py:100-138), values unchanged in scale.
+    Returns (2, N, N, 1), or (3, N, N, 1) with a zero third component for target_dim 3.
+    """
+    G = int(grid_n)
+    if G % N:
+        raise ValueError(f"grid_n={G} must be a multiple of N={N}")
+    rng = np.random.default_rng(seed)
+    noise = rng.standard_normal((2, G, G))
+    f = np.fft.fftfreq(G, L / G)                      # cycles per unit length
+    fh = np.fft.rfftfreq(G, L / G)
+    kabs = np.sqrt(f[:, None] ** 2 + fh[None, :] ** 2)
+    dens = _lognormal_density(kabs, peak_wavenumber)
+    dens[G // 2, :] = 0.0  # Nyquist row and column: no consistent projection there
+    dens[:, G // 2] = 0.0
+    vh = np.fft.rfftn(noise, axes=(1, 2)) * dens
+    kx = f[:, None] + 0.0 * fh[None, :]
+    ky = 0.0 * f[:, None] + fh[None, :]
+    k2 = kabs * kabs
+    inv_k2 = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+    for _ in range(max(1, int(iter))):
+        div = kx * vh[0] + ky * vh[1]                 # projection: v - k (k . v) / |k|^2
+        vh = np.stack([vh[0] - kx * div * inv_k2, vh[1] - ky * div * inv_k2])
+        v = np.fft.irfftn(vh, s=(G, G), axes=(1, 2))
+        vh *= max_velocity / np.sqrt((v * v).sum(0)).max()
+    v0 = _spectral_filter_np(np.fft.irfftn(vh, s=(G, G), axes=(1, 2)), N)[..., None]
+    if target_dim == 3:
+        v0 = np.concatenate([v0, np.zeros((1, N, N, 1))], axis=0)
+    return v0
+

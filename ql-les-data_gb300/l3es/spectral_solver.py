@@ -17,7 +17,7 @@ from time import time
 import numpy as np
 
 from . import _native
-from .init_fields import init_forcing_mask_hit, init_u_hit, init_u_random2d, init_u_tgv, init_u_tgv2d
+from .init_fields import init_forcing_mask_hit, init_u_hit, init_u_kolm, init_u_random2d, init_u_tgv, init_u_tgv2d
 
 EPS = float(np.finfo(np.float64).eps)  # jnp.finfo(float).eps under x64
 
@@ -178,9 +178,11 @@ def _initial_field(case, N, dim, seed, ext):
     if case == "HIT":
         return init_u_hit(N, seed, ext.get("spectrum", "k-5/3"), ext.get("kp", 4.0))
     if case == "Kolm":
-        # the reference initialises from JAX-CFD (init_fields.py:191-212), which is not
-        # available; a seeded band-limited random field (|k| <= 8, KE 0.5) stands in
-        return init_u_random2d(N, seed, ext.get("init_kmax", 8.0), ext.get("init_energy", 0.5))
+        # init_fields.py:191-212 (spectral_solver.py:195-196); init="random2d" selects the
+        # band-limited random-phase field (|k| <= init_kmax, KE init_energy) instead
+        if ext.get("init", "kolm") == "random2d":
+            return init_u_random2d(N, seed, ext.get("init_kmax", 8.0), ext.get("init_energy", 0.5))
+        return init_u_kolm(N, seed=seed, target_dim=3, grid_n=ext.get("kolm_grid", 2048))
     raise ValueError(f"unknown case {case!r}")
 
 
@@ -202,7 +204,7 @@ def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None, forc
     xyz_vis = np.array(np.meshgrid(x, x, np.arange(len_z_vis), indexing="ij")) * L / ckp_N
     if dim == 2:
         xyz_vis = (xyz_vis.T + np.array([0, 0, L - dx])).T
-    init_ext = {k: ext[k] for k in ("spectrum", "kp", "init_kmax", "init_energy") if k in ext}
+    init_ext = {k: ext[k] for k in ("spectrum", "kp", "init", "init_kmax", "init_energy", "kolm_grid") if k in ext}
     plan_ext = {k: ext[k] for k in ("drag", "kolm_k", "kolm_amp", "eps_inj") if k in ext}
     u = _initial_field(case, N, dim, seed, init_ext)
     e_kin_init = 0.5 * np.mean(np.sum(u * u, axis=0))

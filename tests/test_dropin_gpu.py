@@ -164,3 +164,31 @@ def test_particles_to_grid_large_vs_oracle():
     got_sub = T.ur_to_u_dft_wrapper(c, 2 * np.pi, 3)(r[:4096], u[:4096])
     assert _rel(got_sub, sub.reshape(3, -1).T) < 5e-5
     assert got.shape == (c**3, 3)
+
+
+def test_combined_trajectories_to_dataset(tmp_path):
+    """combined() runs (Kolm init on a 256^2 fine grid) write config.json and particle
+    checkpoints that gen_dataset assembles into train/valid/test + metadata."""
+    import json
+
+    from l3es import combined as C
+    from l3es import gen_dataset as GD
+
+    raw = tmp_path / "raw"
+    for seed in (3, 0, 2, 1):
+        C.combined("Kolm", N=32, dim=2, nu=1e-3, t_final=4e-3, dt=1e-3, ckp_N=8, interp_backend="dft",
+                   log_freq=1, ckp_freq=1, dst_path=str(raw / f"traj_{seed}"), seed=seed, kolm_grid=256)
+    cfg = json.loads((raw / "traj_0" / "config.json").read_text())
+    assert cfg["sim"]["case"] == "Kolm" and cfg["sim"]["ckp_N"] == 8 and cfg["com"]["ckp_freq"] == 1
+    dst = tmp_path / "ds"
+    GD.main(["--src_dir", str(raw), "--dst_dir", str(dst), "--split", "2_1_1"])
+    meta = json.loads((dst / "metadata_every1.json").read_text())
+    assert meta["case"] == "KOLM" and meta["dim"] == 2 and meta["num_particles_max"] == 64
+    assert meta["sequence_length_train"] == 5 and meta["num_trajs_train"] == 2
+    ext = ".h5" if GD.h5py is not None else ".npz"
+    (pt, pos, u), = list(GD._read_split(str(dst / f"test{ext}")))
+    last = np.load(raw / "traj_3" / "com" / "step_00004.npz")
+    assert pos.shape == (5, 64, 2)
+    np.testing.assert_array_equal(pos[-1], last["r"].astype(np.float32))
+    np.testing.assert_array_equal(u[-1], last["u"].astype(np.float32))
+    assert all(np.isfinite(meta[k]).all() for k in ("vel_std", "acc_std", "u_std", "au_std"))
