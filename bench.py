@@ -455,6 +455,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     stats = plan.kernel_stats()
     plan.timing(False)
+    plan.check()  # no kernel gave up a bounded wait during the timed or instrumented steps
     # launches of the particle layer per step (crop, prep, 3 grid passes, memset-free
     # binning: count + scan + scatter, gather)
     part_launches = 8 * args.steps if WITH_PARTICLES else 0

@@ -34,6 +34,7 @@ extern "C" {
 #define L3ES_ECUDA (-2)    /* CUDA runtime error (launch, allocation) */
 #define L3ES_ENOMEM (-3)   /* device allocation failed */
 #define L3ES_ESTATE (-4)   /* call not valid for this plan */
+#define L3ES_ETIMEOUT (-5) /* a kernel's bounded wait on its own bulk copies ran out */
 
 #define L3ES_FORCING_NONE 0        /* forcing_type="none" */
 #define L3ES_FORCING_EKIN_TOT 1    /* forcing_type="ekin_tot" (spectral_solver.py:82-112) */
@@ -64,6 +65,11 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out);
 
 /* Releases the plan's device memory. */
 int l3es_plan_destroy(l3es_plan* plan);
+
+/* Waits for the device, then reports L3ES_ETIMEOUT (and clears the flag) if a kernel of
+ * this plan gave up a bounded wait on its own bulk copies since the last check; the
+ * kernel's CTA stopped early, so the results of that call are invalid. */
+int l3es_plan_check(l3es_plan* plan);
 
 /* Per-trajectory ekin_tot target E0 (host array of `batch` doubles);
  * the reference computes it once in set_up_solver (spectral_solver.py:209). */

@@ -20,6 +20,7 @@
 #pragma once
 
 #include "fft_core.cuh"
+#include "tma.cuh"
 
 namespace l3es {
 
@@ -73,28 +74,18 @@ __device__ __forceinline__ void kvec(int kx, int km, int kh, float& k0, float& k
 // x-axis inverse pass. Columns m in [0, NMID*H) of each x-plane; CURL adds the
 // three components of i k x u_hat (np.cross(kkk, u_hat) * 1j) as fields 3..5.
 // ------------------------------------------------------------------------------
+// The six fields of one tile of TW columns m = mid * H + kh (a[c][e]: component c at
+// x row t + T e of column m): x-axis inverse FFT of u and of i k x u, stored to w.
 template <int N, int DIM, bool CURL>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
-kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long long fs,
-       const float2* __restrict__ tw) {
+__device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, int m, bool ok, float2* sm,
+                                              float2* __restrict__ w, long long wofs, long long fs,
+                                              const float2* __restrict__ tw) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
   constexpr int NF = CURL ? 6 : 3;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int m = blockIdx.x * TW + p;
-  const bool ok = m < MC;
-  const long long bofs = (long long)blockIdx.y * 3 * cs;  // batch of trajectories
-  const long long wofs = (long long)blockIdx.y * NF * fs;
   const int kh = m % H;
   const int km = DIM == 3 ? kfull(m / H, N) : 0;
-  float2 a[3][E];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int e = 0; e < E; ++e)
-      a[c][e] = ok ? uh[bofs + c * cs + (long long)(t + T * e) * MC + m] : make_float2(0.f, 0.f);
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
     float2 v[E];
@@ -116,12 +107,103 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
         v[e] = mul_i<kInv>(cr);  // times 1j
       }
     }
-    block_fft<N, E, kInv, TW>(v, sm + p, t, tw, 1);
+    block_fft<N, E, kInv, TW>(v, sm, t, tw, 1);
     if (ok) {
 #pragma unroll
       for (int e = 0; e < E; ++e) w[wofs + f * fs + (long long)(t + T * e) * MC + m] = v[e];
     }
     __syncthreads();
+  }
+}
+
+template <int N, int DIM, bool CURL>
+__global__ void __launch_bounds__(TW * Fft<N>::T)
+kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long long fs,
+       const float2* __restrict__ tw) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
+  constexpr int NMID = DIM == 3 ? N : 1;
+  constexpr int MC = NMID * H;
+  constexpr int NF = CURL ? 6 : 3;
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int m = blockIdx.x * TW + p;
+  const bool ok = m < MC;
+  const long long bofs = (long long)blockIdx.y * 3 * cs;  // batch of trajectories
+  float2 a[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      a[c][e] = ok ? uh[bofs + c * cs + (long long)(t + T * e) * MC + m] : make_float2(0.f, 0.f);
+  kx_inv_fields<N, DIM, CURL>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw);
+}
+
+// Persistent 3D variant: each CTA walks the tiles blockIdx.x, + gridDim.x, ...; the
+// next tile's 3 x N x TW input block (all three components) is fetched by one bulk
+// tensor load into shared memory while the current tile is transformed. The staging
+// block is refilled only after every thread has copied its elements to registers.
+// umap: u_hat as a 3D tensor (MC columns, N rows, 3 * batch components), box
+// (TW, min(N, 256), 3). A wait that times out sets *err and ends the CTA's loop.
+template <int N>
+struct KxTma {
+  static constexpr int NY = N > 256 ? 256 : N;   // rows per bulk load (box limit 256)
+  static constexpr int LOADS = N / NY;
+  static constexpr int STAGE = 3 * N * TW;       // float2 per tile
+  static constexpr int SMEM = (STAGE + xpad_len<TW>(N) * TW) * (int)sizeof(float2);
+  static constexpr unsigned BYTES = (unsigned)STAGE * sizeof(float2);
+};
+
+template <int N, bool CURL>
+__global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
+kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, long long fs,
+           const float2* __restrict__ tw, int ntiles, int* __restrict__ err) {
+  using K = KxTma<N>;
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
+  constexpr int NF = CURL ? 6 : 3;
+  extern __shared__ __align__(128) float2 s_dyn[];
+  float2* stage = s_dyn;            // [load][c][NY rows][TW columns]
+  float2* sm = s_dyn + K::STAGE;    // FFT exchange
+  __shared__ uint64_t bar;
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int batch = blockIdx.y;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int tile) {
+    mbar_arrive_expect_tx(&bar, K::BYTES);
+#pragma unroll
+    for (int l = 0; l < K::LOADS; ++l)
+      tma_load_3d(stage + l * 3 * K::NY * TW, &umap, &bar, tile * TW, l * K::NY, 3 * batch);
+  };
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+  unsigned parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool got = mbar_wait(&bar, parity);
+    if (__syncthreads_or(!got)) {  // every thread leaves together
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      // the load in flight (if any) must land before the CTA's shared memory is released
+      mbar_wait(&bar, parity);
+      return;
+    }
+    parity ^= 1u;
+    float2 a[3][E];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int row = t + T * e;
+        a[c][e] = stage[(((row / K::NY) * 3 + c) * K::NY + row % K::NY) * TW + p];
+      }
+    __syncthreads();  // the staging block is free
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && next < ntiles) {
+      fence_proxy_async_smem();
+      issue(next);
+    }
+    kx_inv_fields<N, 3, CURL>(a, t, tile * TW + p, true, sm + p, w, (long long)batch * NF * fs, fs, tw);
   }
 }
 

@@ -17,7 +17,44 @@ struct DnsOps {
 
   static unsigned line_blocks(long long lines) { return (unsigned)((lines + L::LPC - 1) / L::LPC); }
 
-  static void init_attrs() {}
+  // persistent CTAs of the bulk-copy x inverse pass (0: use kx_inv)
+  static inline int tma_ctas = 0;
+
+  static void init_attrs() {
+    if constexpr (N >= 64) {
+      using K = KxTma<N>;
+      int nb = 0, dev = 0, sms = 0;
+      if (cudaFuncSetAttribute(kx_inv_tma<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM) ==
+              cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kx_inv_tma<N, true>, TX, K::SMEM) == cudaSuccess &&
+          cudaGetDevice(&dev) == cudaSuccess &&
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+        tma_ctas = nb * sms;
+      cudaGetLastError();
+    }
+  }
+
+  // x inverse pass with curl prologue: us -> W (6 fields)
+  template <int DIM>
+  static void x_inverse(const Ctx& c, const float2* us, double bytes, cudaStream_t s) {
+    const long long mc = c.nmid * H;
+    if constexpr (DIM == 3 && N >= 64) {
+      CUtensorMap map;
+      if (tma_ctas > 0 &&
+          tma_encode_3d(&map, us, (unsigned long long)mc, N, 3ull * c.batch, 8ull * mc, 8ull * c.cs, TW,
+                        KxTma<N>::NY, 3)) {
+        const int ntiles = (int)(mc / TW);
+        const int gx = std::max(1, std::min(ntiles, tma_ctas / c.batch));
+        L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                    kx_inv_tma<N, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(map, c.W, c.fs, c.tw,
+                                                                                      ntiles, c.err));
+        return;
+      }
+    }
+    L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                kx_inv<N, DIM, true><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                    us, c.cs, c.W, c.fs, c.tw));
+  }
 
   // us: field the RHS is evaluated on; S: state; out: RK stage field (or du for rk=-1)
   template <int DIM>
@@ -29,9 +66,7 @@ struct DnsOps {
     const double B = c.batch, A = 8.0 * 3.0 * c.cs * B;  // bytes of one 3-component spectrum
     const double Adu = 8.0 * 3.0 * c.ds * B;               // bytes of the truncated DU field
     const double rows = DIM == 3 ? (2.0 * c.kd + 1.0) / N : 1.0;  // kept y rows
-    L3ES_LAUNCH(c, KK_X_INV, 3.0 * A, s,
-                kx_inv<N, DIM, true><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
-                    us, c.cs, c.W, c.fs, c.tw));
+    x_inverse<DIM>(c, us, 3.0 * A, s);
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
                   ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,

@@ -107,6 +107,13 @@ struct KTimer {
     if (_tm) _tm->stop(stream);                                       \
   } while (0)
 
+// Encodes a 3D tiled tensor map (8-byte elements, no swizzle, no interleave) for bulk
+// tensor loads: dims d0 (contiguous), d1, d2 with byte strides s1, s2 and box b0 x b1 x b2.
+// False if the driver entry point is unavailable or the encoding is rejected.
+bool tma_encode_3d(CUtensorMap* map, const void* base, unsigned long long d0, unsigned long long d1,
+                   unsigned long long d2, unsigned long long s1, unsigned long long s2, unsigned b0, unsigned b1,
+                   unsigned b2);
+
 // Geometry + scratch of one plan, handed to the per-N launch wrappers.
 struct Ctx {
   int dim = 3, n = 0, h = 0, batch = 1;
@@ -132,6 +139,7 @@ struct Ctx {
   double* e0 = nullptr;        // [batch] ekin_tot targets
   double* einj = nullptr;      // [batch] scratch e_inj
   float* nu_b = nullptr;       // [batch] viscosity per trajectory
+  int* err = nullptr;          // device error word: nonzero after a kernel wait timed out
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate
   KTimer* timer = nullptr;     // per-launch timing (nullptr = off)

@@ -1,4 +1,6 @@
 // Plan management and the C ABI of the DNS step (include/l3es_gb300.h).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,6 +38,30 @@ const char* kernel_kind_name(int k) {
 }
 
 const Ctx& plan_ctx(const l3es_plan* p) { return p->ctx; }
+
+bool tma_encode_3d(CUtensorMap* map, const void* base, unsigned long long d0, unsigned long long d1,
+                   unsigned long long d2, unsigned long long s1, unsigned long long s2, unsigned b0, unsigned b1,
+                   unsigned b2) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      fn = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode || ((uintptr_t)base & 15u) || (s1 & 15u) || (s2 & 15u)) return false;
+  const cuuint64_t dims[3] = {d0, d1, d2};
+  const cuuint64_t strides[2] = {s1, s2};
+  const cuuint32_t box[3] = {b0, b1, b2};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<void*>(base), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 bool dns_table(int n, DnsTable* out) {
   switch (n) {
@@ -225,6 +251,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.e0, sizeof(double) * B, "e0");
   rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");
   rc = rc ? rc : plan_alloc(p, (void**)&c.nu_b, sizeof(float) * B, "viscosities");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.err, sizeof(int), "error word");
   if (rc != L3ES_OK) {
     plan_free(p);
     delete p;
@@ -236,6 +263,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   if (e == cudaSuccess) e = cudaMemcpy(c.nu_b, nus.data(), sizeof(float) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
+  if (e == cudaSuccess) e = cudaMemset(c.err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     rc = cuda_check(e, "l3es_plan_create");
@@ -244,6 +272,19 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
     return rc;
   }
   *out = p;
+  return L3ES_OK;
+}
+
+int l3es_plan_check(l3es_plan* plan) {
+  if (!plan) return fail(L3ES_EINVAL, "l3es_plan_check: null plan");
+  int h = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, plan->ctx.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(e, "l3es_plan_check");
+  if (h) {
+    cudaMemset(plan->ctx.err, 0, sizeof(int));
+    return fail(L3ES_ETIMEOUT, "l3es_plan_check: a kernel's wait on its bulk copies timed out");
+  }
   return L3ES_OK;
 }
 

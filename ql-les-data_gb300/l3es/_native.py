@@ -23,6 +23,7 @@ _I = ctypes.c_int32
 _SIGNATURES = {
     "l3es_plan_create": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "l3es_plan_destroy": (ctypes.c_int, [_P]),
+    "l3es_plan_check": (ctypes.c_int, [_P]),
     "l3es_plan_set_e0": (ctypes.c_int, [_P, _P, _I]),
     "l3es_plan_workspace_bytes": (ctypes.c_int64, [_P]),
     "l3es_plan_set_nu": (ctypes.c_int, [_P, _P, _I]),
@@ -241,6 +242,11 @@ class Plan:
         self._check_spec(u_hat)
         self._check_phys(u)
         _check(self._lib.l3es_irfftn(self._h, _ptr(u_hat), _ptr(u), _stream(stream)), "l3es_irfftn")
+
+    def check(self) -> None:
+        """Synchronises and raises if one of this plan's kernels gave up a bounded wait
+        on its bulk copies since the last check (the results of that call are invalid)."""
+        _check(self._lib.l3es_plan_check(self._h), "l3es_plan_check")
 
     def kinetic_energy(self, u_hat, out, stream=None) -> None:
         self._check_spec(u_hat)

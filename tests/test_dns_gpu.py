@@ -149,6 +149,7 @@ def test_step3d_large_vs_oracle(n):
     p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3)
     uh = _c64(uh0)
     p.step(uh, 1)
+    p.check()
     assert _rel(uh.cpu().numpy(), uh_ref) < RTOL
     del rng
 
@@ -194,6 +195,7 @@ def test_step3d_512_vs_fp64():
     uh = _c64(uh0)
     del uh0
     p.step(uh, 2)
+    p.check()
     err = float((uh.to(torch.complex128) - ref).abs().max() / ref.abs().max())
     assert err < RTOL
     ke = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -223,3 +225,24 @@ def test_step_energy_equals_kinetic_energy(forcing):
     np.testing.assert_allclose(ke.cpu().numpy(), ref.cpu().numpy(), rtol=1e-6 if forcing == "ekin_tot" else 1e-7)
     if forcing == "ekin_tot":
         np.testing.assert_allclose(ke.cpu().numpy(), 0.5, rtol=1e-6)
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_batched_3d_step_equals_single_plans(n):
+    """A batch of 3 trajectories in one plan (the x pass loads each trajectory's three
+    components as one bulk tensor block) equals three single-trajectory plans, bit for bit."""
+    us = []
+    for b in range(3):
+        u = R.init_u_hit(n, 11 + b, spectrum="k4exp", kp=3.0)
+        us.append(np.fft.rfftn(u * np.sqrt(0.5 / R.kinetic_energy(u)), axes=(1, 2, 3)))
+    pb = _plan(dim=3, n=n, nu=5e-3, dt=2e-3, batch=3, forcing="const_power", kf=2, eps_inj=0.1)
+    uhb = torch.stack([_c64(x) for x in us]).contiguous()
+    pb.step(uhb, 2)
+    pb.check()
+    for b in range(3):
+        p1 = _plan(dim=3, n=n, nu=5e-3, dt=2e-3, forcing="const_power", kf=2, eps_inj=0.1)
+        uh1 = _c64(us[b])
+        p1.step(uh1, 2)
+        p1.check()
+        assert torch.equal(uh1, uhb[b])
+
