@@ -644,33 +644,18 @@ __device__ __forceinline__ void block_sum_store_ff(Ff v, double* partial, int bl
 // modes: P[c][kx + kd][kmid + kd][kh] (3D), P[c][kx + kd][kh] (2D), kh < kt, with
 // zeros for kh > kd.
 // ------------------------------------------------------------------------------
+// One tile of kx_fwd_band: d[c][e] = DU component c at x row t + T e of column kh of
+// middle row kmb (band index); x forward FFT, dealias mask, Leray projection into P.
 template <int N, int DIM>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
-kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
-            const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
-            double inv_n2d, double eps_inj, double* __restrict__ band_scale) {
+__device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int t, int kh, int kmb, int kd, int kt,
+                                                 float2* sm, float2* __restrict__ P, long long pcs, long long bp,
+                                                 const float2* __restrict__ tw) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  constexpr int NMID = DIM == 3 ? N : 1;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
   const int nb = 2 * kd + 1;
-  const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
   const int km = DIM == 3 ? kmb - kd : 0;
-  const int mid = km < 0 ? km + N : km;
-  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
-  const int batch = blockIdx.z;
-  const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
-  if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
-    band_coefficient<DIM>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30,
-                          band_scale + batch);
-  float2 d[3][E];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    block_fft<N, E, kFwd, TW>(d[c], sm + p, t, tw, 1);
+    block_fft<N, E, kFwd, TW>(d[c], sm, t, tw, 1);
     __syncthreads();
   }
 #pragma unroll
@@ -691,6 +676,95 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
     P[o] = make_float2(v0.x - pr * k0, v0.y - pi_ * k0);
     P[o + pcs] = make_float2(v1.x - pr * k1, v1.y - pi_ * k1);
     P[o + 2 * pcs] = make_float2(v2.x - pr * k2, v2.y - pi_ * k2);
+  }
+}
+
+template <int N, int DIM>
+__global__ void __launch_bounds__(TW * Fft<N>::T)
+kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
+            const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
+            double inv_n2d, double eps_inj, double* __restrict__ band_scale) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
+  constexpr int NMID = DIM == 3 ? N : 1;
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
+  const int km = DIM == 3 ? kmb - kd : 0;
+  const int mid = km < 0 ? km + N : km;
+  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
+  const int batch = blockIdx.z;
+  const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
+  if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
+    band_coefficient<DIM>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30,
+                          band_scale + batch);
+  float2 d[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
+  kx_fwd_band_tile<N, DIM>(d, t, kh, kmb, kd, kt, sm + p, P, pcs, bp, tw);
+}
+
+// Persistent 3D variant of kx_fwd_band: tiles (column tile, band row kmb) are walked
+// blockIdx.x, + gridDim.x, ...; the next tile's DU block (TW columns x N x rows x 3
+// components at middle row `mid`) arrives by one 4D bulk tensor load while the current
+// one is transformed. dmap: DU as (kt, N mid, N x, 3 * batch), box (TW, 1, min(N, 256), 3).
+template <int N>
+__global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
+kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2* __restrict__ P, long long pcs,
+                const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
+                double inv_n2d, double eps_inj, double* __restrict__ band_scale, int* __restrict__ err) {
+  using K = KxTma<N>;
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
+  extern __shared__ __align__(128) float2 s_dyn[];
+  float2* stage = s_dyn;
+  float2* sm = s_dyn + K::STAGE;
+  __shared__ uint64_t bar;
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int batch = blockIdx.y;
+  const int ntx = kt / TW, nb = 2 * kd + 1, ntiles = ntx * nb;
+  if (band_kf > 0 && blockIdx.x == 0)
+    band_coefficient<3>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30, band_scale + batch);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int tile) {
+    const int kmb = tile / ntx, x0 = (tile % ntx) * TW;
+    const int km = kmb - kd, mid = km < 0 ? km + N : km;
+    mbar_arrive_expect_tx(&bar, K::BYTES);
+#pragma unroll
+    for (int l = 0; l < K::LOADS; ++l)
+      tma_load_4d(stage + l * 3 * K::NY * TW, &dmap, &bar, x0, mid, l * K::NY, 3 * batch);
+  };
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+  unsigned parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool got = mbar_wait(&bar, parity);
+    if (__syncthreads_or(!got)) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      mbar_wait(&bar, parity);
+      return;
+    }
+    parity ^= 1u;
+    float2 d[3][E];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int row = t + T * e;
+        d[c][e] = stage[(((row / K::NY) * 3 + c) * K::NY + row % K::NY) * TW + p];
+      }
+    __syncthreads();
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && next < ntiles) {
+      fence_proxy_async_smem();
+      issue(next);
+    }
+    kx_fwd_band_tile<N, 3>(d, t, (tile % ntx) * TW + p, tile / ntx, kd, kt, sm + p, P, pcs,
+                           (long long)batch * 3 * pcs, tw);
   }
 }
 

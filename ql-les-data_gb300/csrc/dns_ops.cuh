@@ -20,17 +20,26 @@ struct DnsOps {
   // persistent CTAs of the bulk-copy x inverse pass (0: use kx_inv)
   static inline int tma_ctas = 0;
 
+  static inline int tma_band_ctas = 0;
+
+  // resident CTAs (all SMs) of a persistent kernel with K::SMEM dynamic shared memory
+  template <typename F>
+  static int persistent_ctas(F kernel) {
+    int nb = 0, dev = 0, sms = 0;
+    const int smem = KxTma<N>::SMEM;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, TX, smem) == cudaSuccess &&
+        cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      return nb * sms;
+    cudaGetLastError();
+    return 0;
+  }
+
   static void init_attrs() {
     if constexpr (N >= 64) {
-      using K = KxTma<N>;
-      int nb = 0, dev = 0, sms = 0;
-      if (cudaFuncSetAttribute(kx_inv_tma<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM) ==
-              cudaSuccess &&
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kx_inv_tma<N, true>, TX, K::SMEM) == cudaSuccess &&
-          cudaGetDevice(&dev) == cudaSuccess &&
-          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-        tma_ctas = nb * sms;
-      cudaGetLastError();
+      tma_ctas = persistent_ctas(kx_inv_tma<N, true>);
+      tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
     }
   }
 
@@ -40,9 +49,10 @@ struct DnsOps {
     const long long mc = c.nmid * H;
     if constexpr (DIM == 3 && N >= 64) {
       CUtensorMap map;
-      if (tma_ctas > 0 &&
-          tma_encode_3d(&map, us, (unsigned long long)mc, N, 3ull * c.batch, 8ull * mc, 8ull * c.cs, TW,
-                        KxTma<N>::NY, 3)) {
+      const unsigned long long dims[3] = {(unsigned long long)mc, N, 3ull * c.batch};
+      const unsigned long long strides[2] = {8ull * mc, 8ull * c.cs};
+      const unsigned box[3] = {TW, KxTma<N>::NY, 3};
+      if (tma_ctas > 0 && tma_encode(&map, us, 3, dims, strides, box)) {
         const int ntiles = (int)(mc / TW);
         const int gx = std::max(1, std::min(ntiles, tma_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_INV, bytes, s,
@@ -83,10 +93,27 @@ struct DnsOps {
     const double Ap = 8.0 * 3.0 * c.pcs * B;
     // (block 0 of each trajectory also computes the constant-power coefficient of us)
     const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
-    L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
-                kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
-                    c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
-                    c.eps_inj, c.band));
+    bool band_done = false;
+    if constexpr (DIM == 3 && N >= 64) {
+      CUtensorMap map;
+      const unsigned long long dims[4] = {(unsigned long long)c.kt, N, N, 3ull * c.batch};
+      const unsigned long long strides[3] = {8ull * c.kt, 8ull * N * c.kt, 8ull * c.ds};
+      const unsigned box[4] = {TW, 1, KxTma<N>::NY, 3};
+      if (tma_band_ctas > 0 && tma_encode(&map, c.DU, 4, dims, strides, box)) {
+        const int ntiles = (c.kt / TW) * nb;
+        const int gx = std::max(1, std::min(ntiles, tma_band_ctas / c.batch));
+        L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
+                    kx_fwd_band_tma<N><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
+                        map, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
+                        c.eps_inj, c.band, c.err));
+        band_done = true;
+      }
+    }
+    if (!band_done)
+      L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
+                  kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
+                      c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
+                      c.eps_inj, c.band));
     // rk -1: us -> du; 0: us -> out; 1: us, u0 -> acc, out; 2: us, u0, acc -> acc, out;
     // 3: us, acc -> fin
     const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);

@@ -107,12 +107,12 @@ struct KTimer {
     if (_tm) _tm->stop(stream);                                       \
   } while (0)
 
-// Encodes a 3D tiled tensor map (8-byte elements, no swizzle, no interleave) for bulk
-// tensor loads: dims d0 (contiguous), d1, d2 with byte strides s1, s2 and box b0 x b1 x b2.
-// False if the driver entry point is unavailable or the encoding is rejected.
-bool tma_encode_3d(CUtensorMap* map, const void* base, unsigned long long d0, unsigned long long d1,
-                   unsigned long long d2, unsigned long long s1, unsigned long long s2, unsigned b0, unsigned b1,
-                   unsigned b2);
+// Encodes a tiled tensor map of 8-byte elements (no swizzle, no interleave) for bulk
+// tensor loads: rank dims (dims[0] contiguous), byte strides of dims 1..rank-1 in
+// strides[0..rank-2], box extents `box`. False if the driver entry point is unavailable,
+// an address or stride is not 16-byte aligned, or the encoding is rejected.
+bool tma_encode(CUtensorMap* map, const void* base, int rank, const unsigned long long* dims,
+                const unsigned long long* strides, const unsigned* box);
 
 // Geometry + scratch of one plan, handed to the per-N launch wrappers.
 struct Ctx {

@@ -39,9 +39,8 @@ const char* kernel_kind_name(int k) {
 
 const Ctx& plan_ctx(const l3es_plan* p) { return p->ctx; }
 
-bool tma_encode_3d(CUtensorMap* map, const void* base, unsigned long long d0, unsigned long long d1,
-                   unsigned long long d2, unsigned long long s1, unsigned long long s2, unsigned b0, unsigned b1,
-                   unsigned b2) {
+bool tma_encode(CUtensorMap* map, const void* base, int rank, const unsigned long long* dims,
+                const unsigned long long* strides, const unsigned* box) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -53,12 +52,20 @@ bool tma_encode_3d(CUtensorMap* map, const void* base, unsigned long long d0, un
     }
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
-  if (!encode || ((uintptr_t)base & 15u) || (s1 & 15u) || (s2 & 15u)) return false;
-  const cuuint64_t dims[3] = {d0, d1, d2};
-  const cuuint64_t strides[2] = {s1, s2};
-  const cuuint32_t box[3] = {b0, b1, b2};
-  const cuuint32_t estr[3] = {1, 1, 1};
-  return encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<void*>(base), dims, strides, box, estr,
+  if (!encode || rank < 1 || rank > 5 || ((uintptr_t)base & 15u)) return false;
+  cuuint64_t d[5];
+  cuuint64_t st[4];
+  cuuint32_t b[5], es[5];
+  for (int i = 0; i < rank; ++i) {
+    d[i] = dims[i];
+    b[i] = box[i];
+    es[i] = 1;
+    if (i + 1 < rank) {
+      if (strides[i] & 15u) return false;
+      st[i] = strides[i];
+    }
+  }
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_INT64, (cuuint32_t)rank, const_cast<void*>(base), d, st, b, es,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
