@@ -76,10 +76,14 @@ __device__ __forceinline__ void kvec(int kx, int km, int kh, float& k0, float& k
 // ------------------------------------------------------------------------------
 // The six fields of one tile of TW columns m = mid * H + kh (a[c][e]: component c at
 // x row t + T e of column m): x-axis inverse FFT of u and of i k x u, stored to w.
-template <int N, int DIM, bool CURL>
+// SKIPWX (3D RHS): field 3 (curl_x) is neither transformed nor stored, and fields 1, 2
+// (u_y, u_z) go to the side buffer wx + wxofs (two fields) instead; the y pass
+// (ky_inv_rhs) forms curl_x from them and writes all six fields.
+template <int N, int DIM, bool CURL, bool SKIPWX = false>
 __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, int m, bool ok, float2* sm,
                                               float2* __restrict__ w, long long wofs, long long fs,
-                                              const float2* __restrict__ tw) {
+                                              const float2* __restrict__ tw, float2* __restrict__ wx = nullptr,
+                                              long long wxofs = 0) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
@@ -88,6 +92,7 @@ __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, 
   const int km = DIM == 3 ? kfull(m / H, N) : 0;
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
+    if (SKIPWX && f == 3) continue;
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -109,17 +114,18 @@ __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, 
     }
     block_fft<N, E, kInv, TW>(v, sm, t, tw, 1);
     if (ok) {
+      float2* dst = (SKIPWX && (f == 1 || f == 2)) ? wx + wxofs + (f - 1) * fs : w + wofs + f * fs;
 #pragma unroll
-      for (int e = 0; e < E; ++e) w[wofs + f * fs + (long long)(t + T * e) * MC + m] = v[e];
+      for (int e = 0; e < E; ++e) dst[(long long)(t + T * e) * MC + m] = v[e];
     }
     __syncthreads();
   }
 }
 
-template <int N, int DIM, bool CURL>
+template <int N, int DIM, bool CURL, bool SKIPWX = false>
 __global__ void __launch_bounds__(TW * Fft<N>::T)
 kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long long fs,
-       const float2* __restrict__ tw) {
+       const float2* __restrict__ tw, float2* __restrict__ wx = nullptr) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
@@ -135,7 +141,8 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
 #pragma unroll
     for (int e = 0; e < E; ++e)
       a[c][e] = ok ? uh[bofs + c * cs + (long long)(t + T * e) * MC + m] : make_float2(0.f, 0.f);
-  kx_inv_fields<N, DIM, CURL>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw);
+  kx_inv_fields<N, DIM, CURL, SKIPWX>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw, wx,
+                                      (long long)blockIdx.y * 2 * fs);
 }
 
 // Persistent 3D variant: each CTA walks the tiles blockIdx.x, + gridDim.x, ...; the
@@ -153,10 +160,10 @@ struct KxTma {
   static constexpr unsigned BYTES = (unsigned)STAGE * sizeof(float2);
 };
 
-template <int N, bool CURL>
+template <int N, bool CURL, bool SKIPWX = false>
 __global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
 kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, long long fs,
-           const float2* __restrict__ tw, int ntiles, int* __restrict__ err) {
+           const float2* __restrict__ tw, int ntiles, int* __restrict__ err, float2* __restrict__ wx) {
   using K = KxTma<N>;
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
   constexpr int NF = CURL ? 6 : 3;
@@ -203,7 +210,8 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
       fence_proxy_async_smem();
       issue(next);
     }
-    kx_inv_fields<N, 3, CURL>(a, t, tile * TW + p, true, sm + p, w, (long long)batch * NF * fs, fs, tw);
+    kx_inv_fields<N, 3, CURL, SKIPWX>(a, t, tile * TW + p, true, sm + p, w, (long long)batch * NF * fs, fs, tw,
+                                      wx, (long long)batch * 2 * fs);
   }
 }
 
@@ -234,6 +242,52 @@ ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
       const int k = kfull(ky, N);
       if ((unsigned)(k + kd_store) <= 2u * (unsigned)kd_store) base[(long long)ky * row] = v[e];  // |k| <= kd_store
     }
+  }
+}
+
+// 3D y inverse pass of the RHS: six one-FFT jobs per (column tile, kx plane blockIdx.y,
+// trajectory blockIdx.z), the job index varying fastest (blockIdx.x = 6 tile + job) so
+// the jobs that share an input run side by side and its second read is served by L2:
+//   jobs 0..2: u_x, curl_y, curl_z (fields 0, 4, 5) in place;
+//   job 3: curl_x = FFT_y(i (ky W_z - kz W_y)) -> field 3; after the x pass curl_x is
+//          that pointwise combination (ky, kz are constant along an x pencil), so the x
+//          pass does not store it;
+//   jobs 4, 5: u_y, u_z from the side buffer wx (x-transformed W_y, W_z) -> fields 1, 2.
+// No job writes what another job reads.
+template <int N>
+__global__ void __launch_bounds__(KyCfg<N>::THREADS)
+ky_inv_rhs(float2* __restrict__ w, const float2* __restrict__ wx, long long fs, const float2* __restrict__ tw) {
+  using C = KyCfg<N>;
+  constexpr int E = C::E, T = C::T, TWY = C::TWY, H = N / 2 + 1;
+  __shared__ float2 sm[xpad_len<TWY>(N) * TWY];
+  const int p = threadIdx.x % TWY, t = threadIdx.x / TWY;
+  const int job = blockIdx.x % 6, col = (blockIdx.x / 6) * TWY + p;
+  const bool ok = col < H;
+  const long long plane = (long long)blockIdx.y * N * H + col;
+  float2* wb = w + (long long)blockIdx.z * 6 * fs + plane;
+  const float2* xb = wx + (long long)blockIdx.z * 2 * fs + plane;
+  float2 v[E];
+  if (job == 3) {
+    const float kz = (float)col;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const long long o = (long long)(t + T * e) * H;
+      const float2 wy = ok ? xb[o] : make_float2(0.f, 0.f);
+      const float2 wz = ok ? xb[fs + o] : make_float2(0.f, 0.f);
+      const float ky = (float)kfull(t + T * e, N);
+      v[e] = mul_i<kInv>(make_float2(ky * wz.x - kz * wy.x, ky * wz.y - kz * wy.y));
+    }
+  } else {
+    const float2* src = job < 3 ? wb + (job == 0 ? 0 : (job + 3) * fs) : xb + (job - 4) * fs;
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = ok ? src[(long long)(t + T * e) * H] : make_float2(0.f, 0.f);
+  }
+  block_fft<N, E, kInv, TWY>(v, sm + p, t, tw, 1);
+  if (ok) {
+    const int f = job == 0 ? 0 : job < 3 ? job + 3 : job == 3 ? 3 : job - 3;
+    float2* dst = wb + f * fs;
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[(long long)(t + T * e) * H] = v[e];
   }
 }
 

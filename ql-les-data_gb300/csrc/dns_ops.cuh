@@ -38,7 +38,7 @@ struct DnsOps {
 
   static void init_attrs() {
     if constexpr (N >= 64) {
-      tma_ctas = persistent_ctas(kx_inv_tma<N, true>);
+      tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
     }
   }
@@ -56,14 +56,14 @@ struct DnsOps {
         const int ntiles = (int)(mc / TW);
         const int gx = std::max(1, std::min(ntiles, tma_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_INV, bytes, s,
-                    kx_inv_tma<N, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(map, c.W, c.fs, c.tw,
-                                                                                      ntiles, c.err));
+                    kx_inv_tma<N, true, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
+                        map, c.W, c.fs, c.tw, ntiles, c.err, c.Wx));
         return;
       }
     }
     L3ES_LAUNCH(c, KK_X_INV, bytes, s,
-                kx_inv<N, DIM, true><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
-                    us, c.cs, c.W, c.fs, c.tw));
+                kx_inv<N, DIM, true, DIM == 3><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                    us, c.cs, c.W, c.fs, c.tw, c.Wx));
   }
 
   // us: field the RHS is evaluated on; S: state; out: RK stage field (or du for rk=-1)
@@ -76,11 +76,12 @@ struct DnsOps {
     const double B = c.batch, A = 8.0 * 3.0 * c.cs * B;  // bytes of one 3-component spectrum
     const double Adu = 8.0 * 3.0 * c.ds * B;               // bytes of the truncated DU field
     const double rows = DIM == 3 ? (2.0 * c.kd + 1.0) / N : 1.0;  // kept y rows
-    x_inverse<DIM>(c, us, 3.0 * A, s);
+    // 3D: the x pass stores u_x, curl_y, curl_z in W and u_y, u_z in the side buffer
+    // Wx (curl_x is not stored); the y pass writes all six fields of W
+    x_inverse<DIM>(c, us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
     if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
-                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
-                                                                                         c.tw));
+      L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
+                  ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
     L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
                 line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                     c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));

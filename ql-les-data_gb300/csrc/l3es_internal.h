@@ -15,7 +15,7 @@ namespace l3es {
 
 // Kernel kinds for the per-launch CUDA-event timer (l3es_plan_kernel_stats).
 enum KernelKind {
-  KK_X_INV = 0,     // kx_inv with curl prologue (6 fields)
+  KK_X_INV = 0,     // kx_inv with curl prologue (3D RHS: 5 fields, 2D: 6)
   KK_Y_INV,         // ky_pass inverse
   KK_LINE_CROSS,    // line_cross
   KK_Y_FWD,         // ky_pass forward (truncated)
@@ -128,6 +128,7 @@ struct Ctx {
   long long partial_len = 0;  // doubles per trajectory in `partial`
   float2* tw = nullptr;        // N-point twiddle table + compact table of the N/2-point line FFT
   float2* W = nullptr;         // [batch][6][cs]
+  float2* Wx = nullptr;        // 3D: [batch][2][cs] x-transformed u_y, u_z of the RHS
   float2* DU = nullptr;        // [batch][3][ds]
   float2* Tb = nullptr;        // [batch][3][cs] RK stage field
   float2* C = nullptr;         // [batch][3][cs] RK accumulator

@@ -249,6 +249,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   const std::vector<float2> tw = twiddles(n);
   rc = rc ? rc : plan_alloc(p, (void**)&c.tw, sizeof(float2) * tw.size(), "twiddles");
   rc = rc ? rc : plan_alloc(p, (void**)&c.W, sizeof(float2) * B * 6 * c.fs, "W");
+  if (dim == 3) rc = rc ? rc : plan_alloc(p, (void**)&c.Wx, sizeof(float2) * B * 2 * c.fs, "Wx");
   rc = rc ? rc : plan_alloc(p, (void**)&c.DU, sizeof(float2) * B * 3 * c.ds, "DU");
   rc = rc ? rc : plan_alloc(p, (void**)&c.Tb, sizeof(float2) * B * 3 * c.cs, "stage");
   rc = rc ? rc : plan_alloc(p, (void**)&c.C, sizeof(float2) * B * 3 * c.cs, "accumulator");
