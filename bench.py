@@ -49,8 +49,9 @@ def _ncu_traffic(kernel: str):
     p = os.path.join(ROOT, "profiles", "ncu_full_hit256_stage.md")
     if not os.path.exists(p):
         return None
-    names = {"line_cross": "line_cross<256>", "ky_pass_inv": "ky_pass<256, 1>", "kx_inv_curl": "kx_inv<256, 3, 1>",
-             "rk_update": "k_rk_update<256, 3>", "kx_fwd_band": "kx_fwd_band<256, 3>", "ky_pass_fwd": "ky_pass<256, -1>"}
+    names = {"line_cross": "line_cross<256>", "ky_pass_inv": "ky_inv_rhs<256>", "kx_inv_curl": "kx_inv_tma<256, 1, 1>",
+             "rk_update": "k_rk_update<256, 3>", "kx_fwd_band": "kx_fwd_band_tma<256>",
+             "ky_pass_fwd": "ky_pass<256, (int)-1>"}
     want = names.get(kernel)
     for line in open(p):
         cells = [c.strip() for c in line.strip().strip("|").split("|")]
