@@ -192,16 +192,15 @@ struct DnsOps {
     const double A = 8.0 * 3.0 * c.cs * c.batch;  // bytes of one 3-component spectrum
     const unsigned xb = (unsigned)((mc + TW - 1) / TW);
     const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
-    L3ES_LAUNCH(c, KK_X_INV, 3.0 * A, s,
-                kx_inv<N, DIM, true><<<dim3(xb, c.batch), TX, 0, s>>>(a.us, c.cs, c.W, c.fs, c.tw));
+    // u and curl u lines of the stage field: the forward RHS's x and y inverse passes
+    x_inverse<DIM>(c, a.us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
     L3ES_LAUNCH(c, KK_ADJ_X_INV, 2.0 * A, s,
                 kx_inv_adjproj<N, DIM><<<dim3(xb, c.batch), TX, 0, s>>>(
                     a.g, c.cs, a.gscale, c.kd, Wm, c.fs, c.tw, a.us, a.band_kf2 > 0 ? c.kf : 0, inv_n2d,
                     c.eps_inj, const_cast<double*>(a.band_adj)));
     if (DIM == 3) {
-      L3ES_LAUNCH(c, KK_Y_INV, 4.0 * A, s,
-                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H,
-                                                                                         N / 2, c.tw));
+      L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
+                  ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
       L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
                   ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(Wm, c.fs, H, H, N / 2,
                                                                                          c.tw));
