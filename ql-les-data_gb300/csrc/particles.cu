@@ -161,15 +161,24 @@ __global__ void k_bin_scatter(const double* __restrict__ r, long long np, int nb
 //   u_r[j] = (1 / (n^dim c^dim)) sum_l Re g(l) prod_d phi((x_d/h - l_d) / (w/2))
 //   r_out[j] = (r[j] + dt u_r[j]) mod 2 pi                 (integrator.py:21-23)
 // phi(z) = exp(beta (sqrt(1 - z^2) - 1)); w-point support per axis.
+// Eight lanes per particle (four particles per warp): lane q < W takes support index q
+// of the innermost (contiguous) axis and sums over the W^(dim-1) outer support rows, so
+// the group's loads of one row are W adjacent floats (one L1 wavefront instead of one
+// per particle); the group adds its partial sums by shuffles and lane 0 writes.
 // ------------------------------------------------------------------------------
+constexpr int kGatherLanes = 8;
+
 template <int DIM, int W>
 __global__ void __launch_bounds__(128)
 k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, float beta, double norm,
                const double* __restrict__ r, const int* __restrict__ perm, long long np, double* __restrict__ u_r,
                double dt, double* __restrict__ r_out) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  const long long j = perm ? perm[i] : i;
+  static_assert(W <= kGatherLanes, "one support row per lane");
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = gt / kGatherLanes;
+  const int a = (int)(gt % kGatherLanes);
+  const bool live = i < np;  // every lane stays for the group shuffles
+  const long long j = live ? (perm ? perm[i] : i) : 0;
   const double two_pi = 2.0 * 3.14159265358979323846;
   const double inv_h = n / two_pi;
   float wk[DIM][W];
@@ -178,49 +187,55 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
   for (int d = 0; d < DIM; ++d) {
     // grid coordinate and its offset from the first support point in FP64 (3 FP64
     // operations per axis; FP64 division is avoided: it is slow on this GPU), the W
-    // kernel arguments z = (t - a) / (W/2) in FP32 as before
-    const double xs = r[j * DIM + d] * inv_h;
+    // kernel arguments z = (t - a) / (W/2) in FP32
+    const double xs = (live ? r[j * DIM + d] : 0.0) * inv_h;
     const double l0 = ceil(xs - 0.5 * W);
     const int il0 = (int)l0;
     const float t = (float)(xs - l0);
 #pragma unroll
-    for (int a = 0; a < W; ++a) {
-      const float z = (t - (float)a) * (2.0f / W);
-      const float q = 1.f - z * z;
-      wk[d][a] = q > 0.f ? expf(beta * (sqrtf(q) - 1.f)) : 0.f;
-      id[d][a] = (il0 + a) & (n - 1);  // n is a power of two; two's complement wraps negatives
+    for (int q = 0; q < W; ++q) {
+      const float z = (t - (float)q) * (2.0f / W);
+      const float qq = 1.f - z * z;
+      wk[d][q] = qq > 0.f ? expf(beta * (sqrtf(qq) - 1.f)) : 0.f;
+      id[d][q] = (il0 + q) & (n - 1);  // n is a power of two; two's complement wraps negatives
     }
   }
+  const bool col = live && a < W;
+  float wl = 0.f;  // this lane's innermost-axis weight and grid index
+  int il = 0;
+#pragma unroll
+  for (int q = 0; q < W; ++q)
+    if (q == a) {
+      wl = wk[DIM - 1][q];
+      il = id[DIM - 1][q];
+    }
   double ur[3] = {0.0, 0.0, 0.0};
-  for (int comp = 0; comp < ncomp; ++comp) {
-    const float* gc = gre + comp * gcs;
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    if (comp >= ncomp) break;
+    const float* gc = gre + comp * gcs + il;
     float acc = 0.f;
-    if (DIM == 3) {
+    if (col) {
+      if (DIM == 3) {
 #pragma unroll
-      for (int a = 0; a < W; ++a) {
-        float sa = 0.f;
-#pragma unroll
-        for (int b = 0; b < W; ++b) {
-          const float* row = gc + ((long long)id[0][a] * n + id[1][b]) * n;
+        for (int q0 = 0; q0 < W; ++q0) {
           float sb = 0.f;
 #pragma unroll
-          for (int cc = 0; cc < W; ++cc) sb = fmaf(__ldg(row + id[DIM - 1][cc]), wk[DIM - 1][cc], sb);
-          sa = fmaf(sb, wk[1][b], sa);
+          for (int q1 = 0; q1 < W; ++q1)
+            sb = fmaf(__ldg(gc + ((long long)id[0][q0] * n + id[1][q1]) * n), wk[1][q1], sb);
+          acc = fmaf(sb, wk[0][q0], acc);
         }
-        acc = fmaf(sa, wk[0][a], acc);
-      }
-    } else {
+      } else {
 #pragma unroll
-      for (int a = 0; a < W; ++a) {
-        const float* row = gc + (long long)id[0][a] * n;
-        float sb = 0.f;
-#pragma unroll
-        for (int b = 0; b < W; ++b) sb = fmaf(__ldg(row + id[1][b]), wk[1][b], sb);
-        acc = fmaf(sb, wk[0][a], acc);
+        for (int q0 = 0; q0 < W; ++q0) acc = fmaf(__ldg(gc + (long long)id[0][q0] * n), wk[0][q0], acc);
       }
+      acc *= wl;
     }
+#pragma unroll
+    for (int o = kGatherLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     ur[comp] = (double)acc * norm;
   }
+  if (!live || a != 0) return;
   for (int comp = 0; comp < ncomp; ++comp) u_r[j * ncomp + comp] = ur[comp];
   if (r_out) {
     for (int d = 0; d < DIM; ++d) {
@@ -679,8 +694,9 @@ int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, i
   }
   const double norm = 1.0 / (std::pow((double)p->n, p->dim) * std::pow((double)p->c, p->dim));
   const float beta = (float)p->beta;
+  const unsigned gblk = (unsigned)((np * kGatherLanes + 127) / 128);
 #define L3ES_GATHER(D, W)                                                                                   \
-  k_nufft_gather<D, W><<<pb, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
+  k_nufft_gather<D, W><<<gblk, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
                                           r_out)
   if (p->dim == 3) {
     if (p->w == 6) L3ES_GATHER(3, 6);
