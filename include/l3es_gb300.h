@@ -71,6 +71,11 @@ int l3es_plan_destroy(l3es_plan* plan);
  * kernel's CTA stopped early, so the results of that call are invalid. */
 int l3es_plan_check(l3es_plan* plan);
 
+/* Self-test of the bounded waits used by the bulk-copy kernels: one CTA waits on a
+ * barrier that nothing completes. Returns L3ES_ETIMEOUT when the wait gave up as
+ * designed (about 200 ms; the context stays usable), L3ES_OK if it did not. */
+int l3es_selftest_bounded_wait(void* stream);
+
 /* Per-trajectory ekin_tot target E0 (host array of `batch` doubles);
  * the reference computes it once in set_up_solver (spectral_solver.py:209). */
 int l3es_plan_set_e0(l3es_plan* plan, const double* e0_host, int32_t count);

@@ -296,6 +296,41 @@ int l3es_plan_check(l3es_plan* plan) {
   return L3ES_OK;
 }
 
+namespace l3es {
+// One CTA waits on an mbarrier that expects 16 bytes no copy will deliver (nothing is
+// issued, so nothing is in flight when it gives up); the bounded wait must run out and
+// set *err.
+__global__ void k_wait_selftest(int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar, 16);
+  __syncthreads();
+  const bool got = mbar_wait(&bar, 0);
+  if (__syncthreads_or(!got) && threadIdx.x == 0) *err = 1;
+}
+}  // namespace l3es
+
+int l3es_selftest_bounded_wait(void* stream) {
+  int* d = nullptr;
+  int h = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(int), s);
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 32, 0, s>>>(d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess) return cuda_check(e, "l3es_selftest_bounded_wait");
+  return h ? fail(L3ES_ETIMEOUT, "l3es_selftest_bounded_wait: the wait ran out as expected") : L3ES_OK;
+}
+
 int l3es_plan_destroy(l3es_plan* plan) {
   if (!plan) return L3ES_OK;
   plan_free(plan);

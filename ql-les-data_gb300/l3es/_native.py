@@ -24,6 +24,7 @@ _SIGNATURES = {
     "l3es_plan_create": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "l3es_plan_destroy": (ctypes.c_int, [_P]),
     "l3es_plan_check": (ctypes.c_int, [_P]),
+    "l3es_selftest_bounded_wait": (ctypes.c_int, [_P]),
     "l3es_plan_set_e0": (ctypes.c_int, [_P, _P, _I]),
     "l3es_plan_workspace_bytes": (ctypes.c_int64, [_P]),
     "l3es_plan_set_nu": (ctypes.c_int, [_P, _P, _I]),

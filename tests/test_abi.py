@@ -49,3 +49,4 @@ def test_invalid_arguments_fail_without_gpu():
     assert lib.l3es_plan_create(ctypes.byref(d), ctypes.byref(h)) == -1
     assert b"not supported" in lib.l3es_last_error()
     assert lib.l3es_step(None, None, None, 1, None, None) == -1
+    assert lib.l3es_plan_check(None) == -1

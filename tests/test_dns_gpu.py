@@ -246,3 +246,20 @@ def test_batched_3d_step_equals_single_plans(n):
         p1.check()
         assert torch.equal(uh1, uhb[b])
 
+
+
+def test_bounded_wait_gives_up_and_context_stays_usable():
+    """The mbarrier wait of the bulk-copy kernels is bounded: a wait that nothing
+    completes returns L3ES_ETIMEOUT, and the context still runs a step afterwards."""
+    from l3es import _native
+
+    lib = _native.load()
+    assert lib.l3es_selftest_bounded_wait(None) == -5
+    assert b"ran out" in lib.l3es_last_error()
+    n = 64
+    u0 = R.init_u_hit(n, 2, spectrum="k4exp", kp=3.0)
+    p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3)
+    uh = _c64(np.fft.rfftn(u0, axes=(1, 2, 3)))
+    p.step(uh, 1)
+    p.check()
+    assert torch.isfinite(torch.view_as_real(uh)).all()
