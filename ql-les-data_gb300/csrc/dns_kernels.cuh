@@ -384,8 +384,11 @@ __device__ __forceinline__ void r2c_unpack_regs(const float2 (&v)[E], int t, con
 // Physical u is parked in shared memory (same thread writes and reads it), the
 // cross product accumulates in registers while the curl lines are transformed.
 // ------------------------------------------------------------------------------
+// 4 CTAs (16 warps) per SM up to N = 256: 128 registers, no spills (measured at 256^3:
+// 160.6 vs 166.5 us per launch at 3 CTAs / 168 registers; 5 CTAs spill and take 176 us).
+// N = 512 (256-point lines, one more exchange stage) would spill at 128 and keeps 3.
 template <int N>
-__global__ void __launch_bounds__(LineCfg<N>::THREADS, 3)
+__global__ void __launch_bounds__(LineCfg<N>::THREADS, N <= 256 ? 4 : 3)
 line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, long long ds,
            int kt, int kd, float scale, const float2* __restrict__ twN, int nlines) {
   using C = LineCfg<N>;
