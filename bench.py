@@ -484,7 +484,7 @@ def run_ours(args):
     # device part of the step (DNS step, coarsening, NUFFT + advection, KE) as one graph;
     # the host copies run around each launch on the same stream
     cap = _native.Graph.begin()
-    plan.step(uh, 1, ke=ke_dev, stream=cap)  # KE of the new state from the last stage's sums
+    plan.step(uh, 1, ke=ke_dev, stream=cap)  # the step and the KE of the new state
     ip.set_spectrum(uh, stream=cap)
     ip.interp(r_dev, u_r, backend="nufft", dt=dt, r_out=r_new, stream=cap)
     g_e2e = _native.Graph.end(cap)

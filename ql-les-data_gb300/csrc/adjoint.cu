@@ -74,6 +74,8 @@ int l3es_plan_adjoint_prepare(l3es_plan* plan) {
 int l3es_rhs_vjp(l3es_plan* plan, const void* u_hat, const void* g, void* out, void* stream) {
   if (!plan || !u_hat || !g || !out) return fail(L3ES_EINVAL, "l3es_rhs_vjp: null argument");
   if (out == u_hat) return fail(L3ES_EINVAL, "l3es_rhs_vjp: out must not alias u_hat");
+  if (misaligned16(u_hat) || misaligned16(g) || misaligned16(out))
+    return fail(L3ES_EINVAL, "l3es_rhs_vjp: arrays must be 16-byte aligned");
   int rc = adj_check(plan, "l3es_rhs_vjp");
   if (rc != L3ES_OK) return rc;
   AdjEpi a = adj_epi(plan);
@@ -88,6 +90,8 @@ int l3es_rhs_vjp(l3es_plan* plan, const void* u_hat, const void* g, void* out, v
 int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* stream) {
   if (!plan || !u_hat_n || !lam) return fail(L3ES_EINVAL, "l3es_adjoint_step: null argument");
   if (lam == u_hat_n) return fail(L3ES_EINVAL, "l3es_adjoint_step: lam must not alias u_hat_n");
+  if (misaligned16(u_hat_n) || misaligned16(lam))
+    return fail(L3ES_EINVAL, "l3es_adjoint_step: arrays must be 16-byte aligned");
   int rc = adj_check(plan, "l3es_adjoint_step");
   if (rc != L3ES_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;

@@ -114,6 +114,10 @@ struct KTimer {
 bool tma_encode(CUtensorMap* map, const void* base, int rank, const unsigned long long* dims,
                 const unsigned long long* strides, const unsigned* box);
 
+// Spectra handed to the elementwise and energy kernels are read as float4 (two modes):
+// caller arrays must start on a 16-byte boundary (checked at the C entry points).
+inline bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; }
+
 // Geometry + scratch of one plan, handed to the per-N launch wrappers.
 struct Ctx {
   int dim = 3, n = 0, h = 0, batch = 1;

@@ -126,28 +126,23 @@ static std::vector<float2> twiddles(int n) {
 }
 
 // Parseval kinetic energy: per-block partial sums of w |u_hat|^2 over 3 components.
-// One warp per contiguous half-axis row (h modes), so the weight comes from the lane's
-// position and no index division is needed; each mode's energy is formed in FP32 and
-// accumulated in float-float (Ff), combined across warps and blocks in FP64.
+// The 3 components of a trajectory are one flat array of 3 cs modes read as float4
+// (two modes) in a grid-stride loop, every lane busy; a component holds whole half-axis
+// rows of h modes (cs is a multiple of h and even), so mode i has half-axis index
+// i mod h and weight 1 on the planes 0 and h-1, else 2. Each pair's energy is formed in
+// FP32 and accumulated in float-float (Ff), combined across warps and blocks in FP64.
 __global__ void __launch_bounds__(256)
 k_energy_partial(const float2* __restrict__ uh, long long cs, int h, int nblk, double* __restrict__ partial) {
   const int batch = blockIdx.y;
-  const float2* ub = uh + (long long)batch * 3 * cs;
-  const long long rows = cs / h;
-  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  const float4* ub = reinterpret_cast<const float4*>(uh + (long long)batch * 3 * cs);
+  const unsigned pairs = (unsigned)(3 * cs / 2), uh_ = (unsigned)h;  // 3 cs < 2^32 for N <= 512
   Ff s{0.f, 0.f};
-  for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += (long long)nblk * wpb) {
-    const float2* row = ub + r * h;
-    for (int k = lane; k < h; k += 32) {
-      float e = 0.f;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float2 v = row[c * cs + k];
-        e = fmaf(v.x, v.x, e);
-        e = fmaf(v.y, v.y, e);
-      }
-      s = ff_add(s, (k == 0 || k == h - 1) ? e : 2.f * e);
-    }
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < pairs; q += (unsigned)nblk * blockDim.x) {
+    const float4 v = __ldg(ub + q);
+    const unsigned k0 = (2u * q) % uh_, k1 = k0 + 1u == uh_ ? 0u : k0 + 1u;
+    const float w0 = (k0 == 0u || k0 == uh_ - 1u) ? 1.f : 2.f;
+    const float w1 = (k1 == 0u || k1 == uh_ - 1u) ? 1.f : 2.f;
+    s = ff_add(s, fmaf(w0, fmaf(v.x, v.x, v.y * v.y), w1 * fmaf(v.z, v.z, v.w * v.w)));
   }
   block_sum_store_ff(s, partial, batch * nblk + blockIdx.x);
 }
@@ -385,8 +380,8 @@ const char* l3es_kernel_kind_name(int32_t kind) { return kernel_kind_name(kind);
 
 // per-block partial sums of w |u_hat|^2 into c.partial ([batch][nblk]); returns nblk
 static int energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {
-  const long long rows = c.cs / c.h;  // one warp per row, 8 per block
-  const int nblk = (int)std::min<long long>(c.npartial, (rows + 7) / 8);
+  // 8 blocks of 256 threads per SM of a 152-SM GB300, fewer when the field is small
+  const int nblk = (int)std::min<long long>(std::min<long long>(c.npartial, 8 * 152), (3 * c.cs / 2 + 255) / 256);
   L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,
               k_energy_partial<<<dim3(nblk, c.batch), 256, 0, s>>>(uh, c.cs, c.h, nblk, c.partial));
   return nblk;
@@ -397,6 +392,7 @@ static int energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {
 static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps, double* e_inj_dev, double* ke_dev,
                      void* stream) {
   if (!plan || !u_hat) return fail(L3ES_EINVAL, "l3es_step: null plan or u_hat");
+  if (misaligned16(u_hat)) return fail(L3ES_EINVAL, "l3es_step: u_hat must be 16-byte aligned");
   if (nsteps < 0) return fail(L3ES_EINVAL, "l3es_step: nsteps < 0");
   cudaStream_t s = (cudaStream_t)stream;
   const Ctx& c = plan->ctx;
@@ -463,6 +459,7 @@ int l3es_step_energy(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
 int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream) {
   if (!plan || !u_hat || !du) return fail(L3ES_EINVAL, "l3es_rhs: null argument");
   if (u_hat == du) return fail(L3ES_EINVAL, "l3es_rhs: du must not alias u_hat");
+  if (misaligned16(u_hat) || misaligned16(du)) return fail(L3ES_EINVAL, "l3es_rhs: u_hat and du must be 16-byte aligned");
   const l3es_plan_desc& d = plan->desc;
   EpiParams prm;
   prm.a_dt = 0.f;
@@ -491,6 +488,7 @@ int l3es_irfftn(l3es_plan* plan, const void* u_hat, float* u, void* stream) {
 
 int l3es_kinetic_energy(l3es_plan* plan, const void* u_hat, double* out_dev, void* stream) {
   if (!plan || !u_hat || !out_dev) return fail(L3ES_EINVAL, "l3es_kinetic_energy: null argument");
+  if (misaligned16(u_hat)) return fail(L3ES_EINVAL, "l3es_kinetic_energy: u_hat must be 16-byte aligned");
   const Ctx& c = plan->ctx;
   cudaStream_t s = (cudaStream_t)stream;
   const int nblk = energy_partials(c, (const float2*)u_hat, s);

@@ -176,6 +176,8 @@ class Plan:
 
         if t.dtype != torch.complex64 or tuple(t.shape) != self.spec_shape:
             raise ValueError(f"expected complex64 {self.spec_shape}, got {t.dtype} {tuple(t.shape)}")
+        if not t.is_contiguous() or t.data_ptr() % 16:
+            raise ValueError("spectra must be contiguous and 16-byte aligned (the kernels read two modes at a time)")
 
     def _check_phys(self, t):
         import torch

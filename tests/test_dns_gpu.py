@@ -263,3 +263,29 @@ def test_bounded_wait_gives_up_and_context_stays_usable():
     p.step(uh, 1)
     p.check()
     assert torch.isfinite(torch.view_as_real(uh)).all()
+
+
+def test_misaligned_spectrum_is_refused_not_faulted():
+    """A spectrum that starts 8 bytes off a 16-byte boundary (a view one mode into a
+    buffer) is refused with L3ES_EINVAL before any launch (the elementwise kernels read
+    two modes at a time); the Python binding refuses it too."""
+    import ctypes
+
+    from l3es import _native
+
+    n = 16
+    p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3)
+    numel = int(np.prod(p.spec_shape))
+    buf = torch.zeros(numel + 1, dtype=torch.complex64, device="cuda")
+    bad = buf[1:].view(p.spec_shape)
+    assert bad.data_ptr() % 16 == 8
+    with pytest.raises(ValueError):
+        p.step(bad, 1)
+    lib = _native.load()
+    assert lib.l3es_step(p._h, ctypes.c_void_p(bad.data_ptr()), None, 1, None, None) == -1
+    assert b"aligned" in lib.l3es_last_error()
+    ke = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert lib.l3es_kinetic_energy(p._h, ctypes.c_void_p(bad.data_ptr()), ctypes.c_void_p(ke.data_ptr()), None) == -1
+    good = buf[:numel].view(p.spec_shape)
+    p.step(good, 1)
+    p.check()
