@@ -188,13 +188,16 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
   if (threadIdx.x == 0 && tile < ntiles) issue(tile);
   unsigned parity = 0;
   for (; tile < ntiles; tile += gridDim.x) {
-    const bool got = mbar_wait(&bar, parity);
+    // warp 0 polls the barrier; the other threads check it once after the CTA barrier
+    // (the phase is complete then), which orders the bulk copy's writes before their reads
+    const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;
     if (__syncthreads_or(!got)) {  // every thread leaves together
       if (threadIdx.x == 0) atomicExch(err, 1);
       // the load in flight (if any) must land before the CTA's shared memory is released
       mbar_wait(&bar, parity);
       return;
     }
+    if (threadIdx.x >= 32) mbar_wait(&bar, parity);
     parity ^= 1u;
     float2 a[3][E];
 #pragma unroll
@@ -799,12 +802,13 @@ kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2
   if (threadIdx.x == 0 && tile < ntiles) issue(tile);
   unsigned parity = 0;
   for (; tile < ntiles; tile += gridDim.x) {
-    const bool got = mbar_wait(&bar, parity);
+    const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;  // as in kx_inv_tma
     if (__syncthreads_or(!got)) {
       if (threadIdx.x == 0) atomicExch(err, 1);
       mbar_wait(&bar, parity);
       return;
     }
+    if (threadIdx.x >= 32) mbar_wait(&bar, parity);
     parity ^= 1u;
     float2 d[3][E];
 #pragma unroll
