@@ -21,6 +21,7 @@ struct DnsOps {
   static inline int tma_ctas = 0;
 
   static inline int tma_band_ctas = 0;
+  static inline int tma_plain_ctas = 0;  // x inverse without curl (irfftn)
 
   // resident CTAs (all SMs) of a persistent kernel with K::SMEM dynamic shared memory
   template <typename F>
@@ -40,6 +41,7 @@ struct DnsOps {
     if constexpr (N >= 64) {
       tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
+      tma_plain_ctas = persistent_ctas(kx_inv_tma<N, false>);
     }
   }
 
@@ -138,9 +140,25 @@ struct DnsOps {
     const long long lines = c.nmid * N;
     const float scale = (float)(1.0 / (DIM == 3 ? (double)N * N * N : (double)N * N));
     const double A = 8.0 * 3.0 * c.cs * c.batch, P = 4.0 * 3.0 * c.ps * c.batch;
-    L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
-                kx_inv<N, DIM, false><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
-                    uh, c.cs, c.W, c.fs, c.tw));
+    bool x_done = false;
+    if constexpr (DIM == 3 && N >= 64) {  // persistent, next tile by one bulk tensor load
+      CUtensorMap map;
+      const unsigned long long dims[3] = {(unsigned long long)mc, N, 3ull * c.batch};
+      const unsigned long long strides[2] = {8ull * mc, 8ull * c.cs};
+      const unsigned box[3] = {TW, KxTma<N>::NY, 3};
+      if (tma_plain_ctas > 0 && tma_encode(&map, uh, 3, dims, strides, box)) {
+        const int ntiles = (int)(mc / TW);
+        const int gx = std::max(1, std::min(ntiles, tma_plain_ctas / c.batch));
+        L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
+                    kx_inv_tma<N, false><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(map, c.W, c.fs, c.tw, ntiles,
+                                                                                        c.err, nullptr));
+        x_done = true;
+      }
+    }
+    if (!x_done)
+      L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
+                  kx_inv<N, DIM, false><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
+                      uh, c.cs, c.W, c.fs, c.tw));
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
                   ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
