@@ -97,7 +97,9 @@ struct DnsOps {
     // (block 0 of each trajectory also computes the constant-power coefficient of us)
     const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
     bool band_done = false;
-    if constexpr (DIM == 3 && N >= 64) {
+    // from 256^3: smaller grids have too few band tiles per persistent CTA to pipeline
+    // (measured at 128^3: 9.5 us persistent vs 8.4 us one-shot)
+    if constexpr (DIM == 3 && N >= 256) {
       CUtensorMap map;
       const unsigned long long dims[4] = {(unsigned long long)c.kt, N, N, 3ull * c.batch};
       const unsigned long long strides[3] = {8ull * c.kt, 8ull * N * c.kt, 8ull * c.ds};
