@@ -50,3 +50,22 @@ def test_invalid_arguments_fail_without_gpu():
     assert b"not supported" in lib.l3es_last_error()
     assert lib.l3es_step(None, None, None, 1, None, None) == -1
     assert lib.l3es_plan_check(None) == -1
+
+
+def test_header_is_plain_c99(tmp_path):
+    """The public header compiles as C99 (what a cgo / FFI / C caller includes): a
+    translation unit that takes the address of every declared entry point."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    syms = _header_symbols()
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "l3es_gb300.h"\n#include <stddef.h>\ntypedef void (*l3es_fn)(void);\n'
+                   "l3es_fn l3es_entry_points[] = {\n" + "".join(f"    (l3es_fn)&{s},\n" for s in syms)
+                   + "    NULL};\n")
+    res = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-fsyntax-only",
+                          "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
