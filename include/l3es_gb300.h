@@ -190,9 +190,14 @@ int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r
  * n_fine) to ckp_N and evaluates the exact spectral interpolation at np particles
  * r (float64, (np, dim)) into u_r (float64, (np, dim)). Its one scratch buffer is a
  * fixed 417,792-byte array inside the library: ckp_N <= 32 in 3D, <= 64 in 2D,
- * larger sizes return L3ES_EINVAL. Calls share that array, so calls that overlap
- * on the GPU race; the first call on a device looks up the array's device address
- * and should come before any stream capture on that device. */
+ * larger sizes return L3ES_EINVAL, and so does np above 128 (2^31 - 1). Calls share
+ * that array, so calls that overlap on the GPU race. Every call outside stream
+ * capture looks up the array's device address on the current device; a call on a
+ * capturing stream reuses the address of the last uncaptured call there, so make one
+ * call per device before any capture. CUDA loads device code lazily: the first call
+ * on a device loads the library's module and with it the array, so a host whose
+ * device memory is spoken for makes that first (warm-up) call before handing the
+ * device to its own pool, or sets CUDA_MODULE_LOADING=EAGER. */
 int l3es_interp_dft_noalloc(int32_t dim, int32_t n_fine, int32_t ckp_n, const void* u_hat_fine,
                             const double* r, int64_t np, double* u_r, void* stream);
 

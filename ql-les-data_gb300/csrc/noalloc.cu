@@ -22,9 +22,19 @@
 //    nothing has to start at zero; but two calls whose work overlaps on the GPU
 //    (different streams, or different host threads, without ordering between
 //    them) race on the array and give wrong results;
-//  - the first call on each device looks up the array's device address (the host
-//    symbol itself is only a stand-in and must never be handed to a kernel);
-//    make that first call before any stream capture starts on the device.
+//  - the host symbol of the array is only a stand-in and must never be handed to a
+//    kernel; every call outside stream capture looks up the array's device address
+//    on the current device (cheap), so the address stays right after a
+//    cudaDeviceReset reloads the library's device code; a call made while the
+//    stream is being captured uses the address found by the last call outside
+//    capture on that device, so make one call on each device before any capture;
+//  - CUDA loads a library's device code lazily by default: the first call on a
+//    device (the look-up above) loads the module and so places the array in device
+//    memory. A host whose device memory is spoken for should make that first call
+//    (a warm-up call with a small np) before it hands the device to its own pool,
+//    or run with CUDA_MODULE_LOADING=EAGER;
+//  - np is at most 128 (2^31 - 1) particles (one thread per particle, the grid-x
+//    limit).
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -42,30 +52,36 @@ constexpr long long kNoallocScratchElems = 3LL * 32 * 32 * (32 / 2 + 1);  // 52,
 static __device__ __align__(256) float2 g_noalloc_scratch[kNoallocScratchElems];
 
 constexpr int kMaxDevices = 64;
+constexpr long long kNoallocMaxParticles = 128LL * 2147483647LL;
 static std::atomic<float2*> g_scratch_ptr[kMaxDevices];
 static std::mutex g_scratch_mu;
 
-// Device address of g_noalloc_scratch on the current device (looked up once per
-// device; the lookup is the first call's set-up step).
-static int noalloc_scratch(float2** out) {
+// Device address of g_noalloc_scratch on the current device: looked up on every call
+// outside stream capture (after a cudaDeviceReset the module is reloaded and the
+// array may move), the cached value of this device while `stream` is capturing.
+static int noalloc_scratch(cudaStream_t stream, float2** out) {
   int dev = -1;
   int rc = cuda_check(cudaGetDevice(&dev), "l3es_interp_dft_noalloc: cudaGetDevice");
   if (rc != L3ES_OK) return rc;
   if (dev < 0 || dev >= kMaxDevices) return fail(L3ES_ESTATE, "l3es_interp_dft_noalloc: device index out of range");
-  float2* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-  if (!p) {
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    p = g_scratch_ptr[dev].load(std::memory_order_relaxed);
-    if (!p) {
-      void* addr = nullptr;
-      rc = cuda_check(cudaGetSymbolAddress(&addr, g_noalloc_scratch),
-                      "l3es_interp_dft_noalloc: cudaGetSymbolAddress(scratch)");
-      if (rc != L3ES_OK) return rc;
-      p = static_cast<float2*>(addr);
-      g_scratch_ptr[dev].store(p, std::memory_order_release);
-    }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  rc = cuda_check(cudaStreamIsCapturing(stream, &cap), "l3es_interp_dft_noalloc: cudaStreamIsCapturing");
+  if (rc != L3ES_OK) return rc;
+  if (cap != cudaStreamCaptureStatusNone) {
+    float2* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!p)
+      return fail(L3ES_ESTATE,
+                  "l3es_interp_dft_noalloc: the first call on a device must come before any stream capture");
+    *out = p;
+    return L3ES_OK;
   }
-  *out = p;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  void* addr = nullptr;
+  rc = cuda_check(cudaGetSymbolAddress(&addr, g_noalloc_scratch),
+                  "l3es_interp_dft_noalloc: cudaGetSymbolAddress(scratch)");
+  if (rc != L3ES_OK) return rc;
+  g_scratch_ptr[dev].store(static_cast<float2*>(addr), std::memory_order_release);
+  *out = static_cast<float2*>(addr);
   return L3ES_OK;
 }
 
@@ -80,17 +96,19 @@ extern "C" int l3es_interp_dft_noalloc(int32_t dim, int32_t n_fine, int32_t ckp_
   if (ckp_n < 2 || (ckp_n & (ckp_n - 1)) != 0 || n_fine < ckp_n || (n_fine & (n_fine - 1)) != 0)
     return fail(L3ES_EINVAL, "l3es_interp_dft_noalloc: need powers of two with 2 <= ckp_N <= N");
   if (np < 0) return fail(L3ES_EINVAL, "l3es_interp_dft_noalloc: np < 0");
+  if (np > kNoallocMaxParticles)
+    return fail(L3ES_EINVAL, "l3es_interp_dft_noalloc: np above 128 (2^31 - 1), the one-thread-per-particle grid limit");
   const int c = ckp_n, hc = c / 2 + 1;
   const long long hcs = dim == 3 ? (long long)c * c * hc : (long long)c * hc;
   if (3 * hcs > kNoallocScratchElems || (dim == 2 && c > 64))
     return fail(L3ES_EINVAL, "l3es_interp_dft_noalloc: ckp_N=" + std::to_string(c) + " in " + std::to_string(dim) +
                                  "D is above the limit of the fixed " + std::to_string(kNoallocScratchElems * 8) +
                                  "-byte scratch (3D ckp_N <= 32, 2D ckp_N <= 64)");
+  cudaStream_t s = (cudaStream_t)stream;
   float2* hh = nullptr;
-  int rc = noalloc_scratch(&hh);
+  int rc = noalloc_scratch(s, &hh);
   if (rc != L3ES_OK) return rc;
   if (np == 0) return L3ES_OK;
-  cudaStream_t s = (cudaStream_t)stream;
   const int N = n_fine;
   const long long cs = dim == 3 ? (long long)N * N * (N / 2 + 1) : (long long)N * (N / 2 + 1);
   const float scale = (float)std::pow((double)c / N, dim);

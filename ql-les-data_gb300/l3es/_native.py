@@ -472,8 +472,22 @@ def interp_dft_noalloc(dim: int, n_fine: int, ckp_n: int, u_hat_fine, r, u_r, st
     the library's fixed scratch limits ckp_n to 32 (3D) or 64 (2D)."""
     import torch
 
+    dim, n_fine, ckp_n = int(dim), int(n_fine), int(ckp_n)
+    if dim not in (2, 3):
+        raise ValueError("dim must be 2 or 3")
     if r.dtype != torch.float64 or u_r.dtype != torch.float64 or r.shape != u_r.shape:
         raise ValueError("positions and velocities are float64 (np, dim)")
+    if r.dim() != 2 or r.shape[1] != dim:
+        raise ValueError(f"positions and velocities must be (np, {dim}) arrays, got {tuple(r.shape)}")
+    if n_fine < 2 or n_fine & (n_fine - 1):
+        raise ValueError("n_fine must be a power of two")
+    want = 3 * n_fine ** (dim - 1) * (n_fine // 2 + 1)
+    if u_hat_fine.dtype != torch.complex64 or u_hat_fine.numel() != want or not u_hat_fine.is_contiguous():
+        raise ValueError(f"u_hat_fine must be a contiguous complex64 half spectrum of {want} values "
+                         f"(3, {n_fine}{', ' + str(n_fine) if dim == 3 else ''}, {n_fine // 2 + 1}), "
+                         f"got {u_hat_fine.dtype} {tuple(u_hat_fine.shape)}")
+    if not (r.is_contiguous() and u_r.is_contiguous()):
+        raise ValueError("positions and velocities must be contiguous")
     _check(load().l3es_interp_dft_noalloc(int(dim), int(n_fine), int(ckp_n), _ptr(u_hat_fine), _ptr(r),
                                           int(r.shape[0]), _ptr(u_r), _stream(stream)), "l3es_interp_dft_noalloc")
 

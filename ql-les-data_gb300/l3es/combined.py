@@ -57,8 +57,7 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
 
     u, u_hat, xyz_vis, dx_dns, integrate_fn, L, fft_axes, ek_ini, e_inj = set_up_solver(
         N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target, forcing_type, rejit, **ext)
-    print(f"{'#' * 79}\nSimulation with N={N}, nu={nu}, t_final={t_final}, dt={dt}",
-          f"E_kin_init={ek_ini:.3f}\n{'#' * 79}")
+    print(f"[l3es_gb300] {case} + particles dim={dim} N={N} nu={nu} dt={dt} t_final={t_final} KE0={ek_ini:.4f}")
     r, comp_rho, _, _, _, _, _ = set_up_integrator(state_0_path, dim, ckp_N, dft_splits, u_ref, interp_backend)
     npart = r.shape[0]
     ip = _interp_plan(dim, N, ckp_N, np_max=npart)
@@ -105,8 +104,8 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
             dt_est = float(dt_from_stats(st, dx_dns, nu))
             with open(diagnostics_path, "a", newline="") as f:
                 csv.writer(f).writerow([i, float(i * dt), umax, e_kin, dt_est, float(e_inj), rho_max])
-            print(f"Step {i}/{tstep_max}, u_max = {umax:.3f}, E_kin = {e_kin:.3f}, "
-                  f"dt_est = {dt_est:.5f}, E_inj = {float(e_inj):.3f}, rho_max = {rho_max:.3f}")
+            print(f"[{i:>7d}/{tstep_max}] umax {umax:.4f}  KE {e_kin:.4f}  dt_cfl {dt_est:.5f}  "
+                  f"e_inj {float(e_inj):.4f}  rho_max {rho_max:.4f}")
         if is_ckp:
             np.savez(os.path.join(int_path, f"step_{i:05d}.npz"), r=r.cpu().numpy(), u=u_r.cpu().numpy())
         r, r_next = r_next, r
@@ -115,8 +114,7 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
         avg = float(e_acc) / tstep_max
         if avg > 0:
             tau = 1.0 / (avg * kf**2) ** (1 / 3)
-            print(f"Eddy turnover time =            {tau:.3f}")
-            print(f"Number of eddy turnover times = {t_final / tau:.3f}")
-            print(f"Average energy injected =       {avg:.3f}")
-    print(f"t_tot = {time() - t0:.3f}, t_sim = {t_sim}, t_int = {t_int:.3f}")
+            print(f"[l3es_gb300] forced HIT: mean injection {avg:.4f}, large-eddy time {tau:.3f} "
+                  f"({t_final / tau:.2f} of them simulated)")
+    print(f"[l3es_gb300] wall {time() - t0:.2f} s: stepping {t_sim:.2f} s, particles {t_int:.2f} s")
     return u, u_hat, r

@@ -230,7 +230,7 @@ def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None, forc
     t0 = time()
     u_t, u_hat, e_inj = integrate_fn(u_t, u_hat)
     torch.cuda.synchronize()
-    print(f"Compilation time {time() - t0:.3f}")
+    print(f"[l3es_gb300] warm-up step {time() - t0:.3f} s")
     return u_t, u_hat, xyz_vis, dx, integrate_fn, L, fft_axes, e_kin_init, e_inj
 
 
@@ -267,8 +267,7 @@ def simulate(case="TGV3D", N=64, dim=3, nu=0.000625, t_final=0.1, t_burnin=0.0, 
     with open(diagnostics_path, "w", newline="") as f:
         csv.writer(f).writerow(["step", "time", "umax", "ekin", "dt_est", "e_inj"])
     e_inj_acc = torch.zeros((), dtype=torch.float64, device="cuda")
-    print(f"{'#' * 79}\nSimulation with N={N}, nu={nu}, t_final={t_final}, dt={dt}, ",
-          f"E_kin_init={e_kin_init:.3f}\n{'#' * 79}")
+    print(f"[l3es_gb300] {case} dim={dim} N={N} nu={nu} dt={dt} t_final={t_final} KE0={e_kin_init:.4f}")
     t_sim, t0 = 0.0, time()
     tstep_max = round(t_final / dt)
     burnin_steps = round(t_burnin / dt) if t_burnin > 0 else 0
@@ -289,8 +288,8 @@ def simulate(case="TGV3D", N=64, dim=3, nu=0.000625, t_final=0.1, t_burnin=0.0, 
             dt_est = float(dt_from_stats(st, dx, nu))
             with open(diagnostics_path, "a", newline="") as f:
                 csv.writer(f).writerow([i, float(i * dt), umax, e_kin, dt_est, float(e_inj)])
-            print(f"Step {i}/{tstep_max}, u_max = {umax:.3f}, E_kin = {e_kin:.3f}, "
-                  f"dt_est = {dt_est:.5f}, E_inj = {float(e_inj):.3f}")
+            print(f"[{i:>7d}/{tstep_max}] umax {umax:.4f}  KE {e_kin:.4f}  dt_cfl {dt_est:.5f}  "
+                  f"e_inj {float(e_inj):.4f}")
         if i == burnin_steps:
             write_u(u, i, dst_path, N, suffix="_burnin")
         if i % ckp_freq == 0 and i >= burnin_steps:
@@ -299,20 +298,17 @@ def simulate(case="TGV3D", N=64, dim=3, nu=0.000625, t_final=0.1, t_burnin=0.0, 
         avg = float(e_inj_acc) / i
         if avg > 0:
             tau = 1.0 / (avg * kf**2) ** (1 / 3)
-            print(f"Eddy turnover time =            {tau:.3f}")
-            print(f"Number of eddy turnover times = {t_final / tau:.3f}")
-            print(f"Average energy injected =       {avg:.3f}")
             kmax = np.sqrt(2) * N / 3
             eta = (nu**3 / avg) ** 0.25
-            print(f"eta=                            {eta:.3f}")
-            print(f"kmax*eta =                      {kmax * eta:.3f}")
-            if e_kin is not None:
-                print(f"Re_lambda =                     {np.sqrt(20 * e_kin**2 / (3 * nu * avg)):.3f}")
-    print(f"t_tot = {time() - t0:.3f}, t_sim = {t_sim:.3f}")
+            re_l = f", Re_lambda {np.sqrt(20 * e_kin**2 / (3 * nu * avg)):.2f}" if e_kin is not None else ""
+            print(f"[l3es_gb300] forced HIT: mean injection {avg:.4f}, large-eddy time {tau:.3f} "
+                  f"({t_final / tau:.2f} of them simulated), Kolmogorov scale {eta:.4f}, "
+                  f"kmax*eta {kmax * eta:.3f}{re_l}")
+    print(f"[l3es_gb300] wall {time() - t0:.2f} s, of which stepping {t_sim:.2f} s")
     if t_final == 0.1 and case == "TGV3D":
         e_kin = float(_field_stats(u, dim)[3])
         assert round(e_kin - 0.124953117517, 2) == 0, f"e_kin = {e_kin}"
-        print("Assert passed!")
+        print("[l3es_gb300] TGV3D kinetic energy matches the spectralDNS value")
     return u, u_hat
 
 

@@ -1,7 +1,7 @@
 """Generate golden input/output vectors from the reference's own source files.
 
 Run here (not on the GPU machine, where the reference is absent):
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 The reference (tumaer/ql-les-data, package ``l3es``) needs jax 0.4.29, which is not
 installed, so ``jax_numpy_shim`` supplies a NumPy-backed ``jax.numpy`` (FP64, the
@@ -173,4 +173,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

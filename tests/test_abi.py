@@ -69,3 +69,35 @@ def test_header_is_plain_c99(tmp_path):
     res = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-fsyntax-only",
                           "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+def test_noalloc_wrapper_rejects_bad_inputs_before_launching():
+    """The Python wrapper of the allocation-free entry point validates shapes, dtypes
+    and sizes on the host and raises before anything reaches the library (CPU tensors:
+    a launch would fail differently)."""
+    import torch
+
+    from l3es import _native
+
+    n, c = 16, 8
+    uh3 = torch.zeros(3, n, n, n // 2 + 1, dtype=torch.complex64)
+    r3 = torch.zeros(10, 3, dtype=torch.float64)
+    bad = [
+        # positions of the wrong dimension (reads past the end of r in the kernel)
+        dict(dim=3, uh=uh3, r=torch.zeros(10, 2, dtype=torch.float64)),
+        # spectrum of a larger grid than n_fine says, and of a smaller one
+        dict(dim=3, uh=torch.zeros(3, 2 * n, 2 * n, n + 1, dtype=torch.complex64), r=r3),
+        dict(dim=3, uh=torch.zeros(3, n, n, n // 2, dtype=torch.complex64), r=r3),
+        # wrong dtype of the spectrum
+        dict(dim=3, uh=torch.zeros(3, n, n, n // 2 + 1, dtype=torch.complex128), r=r3),
+        # non-contiguous spectrum
+        dict(dim=3, uh=torch.zeros(3, n, n, n + 2, dtype=torch.complex64)[..., ::2], r=r3),
+        # a 2D call with a 3D spectrum
+        dict(dim=2, uh=uh3, r=torch.zeros(10, 2, dtype=torch.float64)),
+        # float32 positions
+        dict(dim=3, uh=uh3, r=torch.zeros(10, 3, dtype=torch.float32)),
+    ]
+    for case in bad:
+        out = torch.zeros(case["r"].shape, dtype=torch.float64)
+        with pytest.raises(ValueError):
+            _native.interp_dft_noalloc(case["dim"], n, c, case["uh"], case["r"], out)

@@ -56,6 +56,26 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert _rel(got.cpu().numpy(), ref) < RTOL
 
 
+def test_noalloc_ignores_the_previous_calls_scratch_and_allocates_nothing():
+    """A call at the same size right after a call on a different field gives that
+    field's answer (stale scratch would show), and a call whose inputs and outputs
+    already exist leaves the device's free memory unchanged."""
+    from l3es import _native
+
+    uh_a, r = _case(3, 64, 5)
+    uh_b, _ = _case(3, 64, 6)
+    ref_b = _with_plan(3, 64, 32, uh_b, r)
+    got = torch.empty_like(r)
+    _native.interp_dft_noalloc(3, 64, 32, uh_a, r, got)  # fills the scratch with field a
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    _native.interp_dft_noalloc(3, 64, 32, uh_b, r, got)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert _rel(got.cpu().numpy(), ref_b) < RTOL
+    assert free1 == free0
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     from l3es import _native
 
