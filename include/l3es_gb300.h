@@ -35,6 +35,7 @@ extern "C" {
 #define L3ES_ENOMEM (-3)   /* device allocation failed */
 #define L3ES_ESTATE (-4)   /* call not valid for this plan */
 #define L3ES_ETIMEOUT (-5) /* a kernel's bounded wait on its own bulk copies ran out */
+#define L3ES_ENONFINITE (-6) /* a step produced NaN or infinite values (blow-up) */
 
 #define L3ES_FORCING_NONE 0        /* forcing_type="none" */
 #define L3ES_FORCING_EKIN_TOT 1    /* forcing_type="ekin_tot" (spectral_solver.py:82-112) */
@@ -66,9 +67,12 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out);
 /* Releases the plan's device memory. */
 int l3es_plan_destroy(l3es_plan* plan);
 
-/* Waits for the device, then reports L3ES_ETIMEOUT (and clears the flag) if a kernel of
- * this plan gave up a bounded wait on its own bulk copies since the last check; the
- * kernel's CTA stopped early, so the results of that call are invalid. */
+/* Waits for the device, then reports (and clears) the plan's device error flags set
+ * since the last check: L3ES_ETIMEOUT if a kernel gave up a bounded wait on its own
+ * bulk copies (that CTA stopped early, so the results of that call are invalid), else
+ * L3ES_ENONFINITE if a step wrote a NaN or infinity into the state (blow-up; the
+ * reference shows it only through its umax / dt_est log columns,
+ * l3es/spectral_solver.py:318-324). */
 int l3es_plan_check(l3es_plan* plan);
 
 /* Self-test of the bounded waits used by the bulk-copy kernels: one CTA waits on a

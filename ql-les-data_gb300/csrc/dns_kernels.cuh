@@ -26,6 +26,10 @@ namespace l3es {
 
 constexpr int TW = 8;  // pencils (columns) per CTA in the strided x / y passes
 
+// Bits of a plan's device error word (reported and cleared by l3es_plan_check).
+constexpr int kErrTimeout = 1;    // a bounded wait on a bulk copy ran out
+constexpr int kErrNonFinite = 2;  // the RK update produced a NaN or infinity
+
 // Half-axis line passes: one line (an M = N/2 point complex FFT) per T = M/8
 // threads, all in one warp, so the FFT exchanges use __syncwarp only and warps run
 // independently. 4 warps per CTA.
@@ -192,7 +196,7 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
     // (the phase is complete then), which orders the bulk copy's writes before their reads
     const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;
     if (__syncthreads_or(!got)) {  // every thread leaves together
-      if (threadIdx.x == 0) atomicExch(err, 1);
+      if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
       // the load in flight (if any) must land before the CTA's shared memory is released
       mbar_wait(&bar, parity);
       return;
@@ -804,7 +808,7 @@ kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2
   for (; tile < ntiles; tile += gridDim.x) {
     const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;  // as in kx_inv_tma
     if (__syncthreads_or(!got)) {
-      if (threadIdx.x == 0) atomicExch(err, 1);
+      if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
       mbar_wait(&bar, parity);
       return;
     }
@@ -898,11 +902,14 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
   return nv;
 }
 
+// The last stage (rk 3) also flags a non-finite value of the new state in *err
+// (kErrNonFinite): the blow-up check of the drivers, one add and one compare per
+// thread, no extra pass.
 template <int N, int DIM>
 __global__ void __launch_bounds__(256)
 k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const float2* us, const float2* u0,
             float2* acc, float2* out, float2* fin, long long cs, EpiParams prm,
-            const double* __restrict__ band_scale, const float* __restrict__ nu_b) {
+            const double* __restrict__ band_scale, const float* __restrict__ nu_b, int* __restrict__ err) {
   const int batch = blockIdx.y;
   prm.nu = nu_b[batch];  // per-trajectory viscosity
   const long long pairs = 3 * cs / 2;
@@ -931,6 +938,9 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
       reinterpret_cast<float4*>(out + bo)[q] = make_float4(nv0.x, nv0.y, nv1.x, nv1.y);
     } else {
       reinterpret_cast<float4*>(fin + bo)[q] = make_float4(nv0.x, nv0.y, nv1.x, nv1.y);
+      // a sum of values is non-finite if one of them is (or if it overflows, which a
+      // field near FLT_MAX is about to do anyway)
+      if (!isfinite((nv0.x + nv0.y) + (nv1.x + nv1.y))) atomicOr(err, kErrNonFinite);
     }
   }
 }

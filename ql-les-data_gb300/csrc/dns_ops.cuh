@@ -125,7 +125,7 @@ struct DnsOps {
     const long long pairs = 3 * c.cs / 2;
     L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
                 k_rk_update<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(
-                    c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm, c.band, c.nu_b));
+                    c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm, c.band, c.nu_b, c.err));
   }
 
   static void stage(const Ctx& c, const float2* us, float2* S, float2* out, int rk, const EpiParams& prm,

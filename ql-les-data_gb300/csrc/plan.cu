@@ -286,7 +286,11 @@ int l3es_plan_check(l3es_plan* plan) {
   if (e != cudaSuccess) return cuda_check(e, "l3es_plan_check");
   if (h) {
     cudaMemset(plan->ctx.err, 0, sizeof(int));
-    return fail(L3ES_ETIMEOUT, "l3es_plan_check: a kernel's wait on its bulk copies timed out");
+    if (h & kErrTimeout)
+      return fail(L3ES_ETIMEOUT, std::string("l3es_plan_check: a kernel's wait on its bulk copies timed out") +
+                                     ((h & kErrNonFinite) ? " (and the state held non-finite values)" : ""));
+    return fail(L3ES_ENONFINITE, "l3es_plan_check: a step produced non-finite values (the flow blew up; "
+                                 "a smaller dt or a larger viscosity is needed)");
   }
   return L3ES_OK;
 }
@@ -305,7 +309,7 @@ __global__ void k_wait_selftest(int* err) {
   if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar, 16);
   __syncthreads();
   const bool got = mbar_wait(&bar, 0);
-  if (__syncthreads_or(!got) && threadIdx.x == 0) *err = 1;
+  if (__syncthreads_or(!got) && threadIdx.x == 0) *err = kErrTimeout;
 }
 }  // namespace l3es
 

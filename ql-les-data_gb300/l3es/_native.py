@@ -114,10 +114,18 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     return lib
 
 
+ENONFINITE = -6  # L3ES_ENONFINITE
+
+
+class NonFiniteError(RuntimeError):
+    """A step wrote NaN or infinite values into the state (the flow blew up)."""
+
+
 def _check(rc: int, what: str) -> None:
     if rc != 0:
         msg = load().l3es_last_error().decode()
-        raise RuntimeError(f"{what} failed ({rc}): {msg}")
+        cls = NonFiniteError if rc == ENONFINITE else RuntimeError
+        raise cls(f"{what} failed ({rc}): {msg}")
 
 
 def _stream(stream=None) -> int:
@@ -248,7 +256,9 @@ class Plan:
 
     def check(self) -> None:
         """Synchronises and raises if one of this plan's kernels gave up a bounded wait
-        on its bulk copies since the last check (the results of that call are invalid)."""
+        on its bulk copies since the last check (RuntimeError: the results of that call
+        are invalid), or if a step wrote NaN or infinite values into the state
+        (NonFiniteError: the flow blew up). Clears the flags."""
         _check(self._lib.l3es_plan_check(self._h), "l3es_plan_check")
 
     def kinetic_energy(self, u_hat, out, stream=None) -> None:

@@ -27,7 +27,7 @@ import numpy as np
 
 from .integrator import set_up_integrator
 from .relax import relax_velocity_wrapper
-from .spectral_solver import _field_stats, dt_from_stats, set_up_solver, _torch
+from .spectral_solver import _check_blowup, _field_stats, dt_from_stats, set_up_solver, _torch
 from .utils import _interp_plan, write_u
 
 
@@ -79,6 +79,7 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
         u, u_hat, e_inj = integrate_fn(u, u_hat)
         torch.cuda.synchronize()
         t_sim += time() - t_temp
+        _check_blowup(integrate_fn, i)
         e_acc += e_inj
 
         t_temp = time()

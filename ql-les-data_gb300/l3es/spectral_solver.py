@@ -281,6 +281,7 @@ def simulate(case="TGV3D", N=64, dim=3, nu=0.000625, t_final=0.1, t_burnin=0.0, 
         u, u_hat, e_inj = integrate_fn(u, u_hat)
         torch.cuda.synchronize()
         t_sim += time() - t_temp
+        _check_blowup(integrate_fn, i)
         e_inj_acc += e_inj
         if i % log_freq == 0:
             st = _field_stats(u, dim).cpu().numpy()
@@ -310,6 +311,20 @@ def simulate(case="TGV3D", N=64, dim=3, nu=0.000625, t_final=0.1, t_burnin=0.0, 
         assert round(e_kin - 0.124953117517, 2) == 0, f"e_kin = {e_kin}"
         print("[l3es_gb300] TGV3D kinetic energy matches the spectralDNS value")
     return u, u_hat
+
+
+def _check_blowup(integrate_fn, step):
+    """Raises NonFiniteError naming the step if the last step of the driver's step
+    function wrote NaN or infinite values (the plan's device flag, set by the final
+    RK update; the reference shows a blow-up only in its umax / dt_est log columns,
+    spectral_solver.py:318-324). The drivers synchronise every step anyway."""
+    p = getattr(integrate_fn, "plan", None)
+    if p is None:
+        return
+    try:
+        p.check()
+    except _native.NonFiniteError as e:
+        raise _native.NonFiniteError(f"step {step}: {e}") from None
 
 
 def dt_from_stats(stats, dx, nu, cfl=1.0):

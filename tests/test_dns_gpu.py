@@ -289,3 +289,31 @@ def test_misaligned_spectrum_is_refused_not_faulted():
     good = buf[:numel].view(p.spec_shape)
     p.step(good, 1)
     p.check()
+
+
+@pytest.mark.parametrize("dim,n", [(3, 32), (2, 64)])
+def test_nonfinite_state_is_reported_and_cleared(dim, n):
+    """Blow-up detection: a NaN written into u_hat on the host before the call spreads
+    through the step; the final RK update flags it and l3es_plan_check reports
+    L3ES_ENONFINITE (NonFiniteError), once. A finite state then steps cleanly. (A NaN
+    in the data neither traps nor hangs the GPU: the kernels only add and multiply it.)"""
+    from l3es import _native
+
+    rng = np.random.default_rng(7)
+    shape = (3, n, n, n) if dim == 3 else (3, n, n, 1)
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    u = 0.1 * rng.standard_normal(shape)
+    p = _plan(dim=dim, n=n, nu=5e-3, dt=1e-3)
+    spec = np.fft.rfftn(u, axes=axes).reshape(p.spec_shape)
+    bad = spec.copy()
+    bad[(0,) * len(p.spec_shape[:-1]) + (1,)] = np.nan
+    uh = _c64(bad)
+    p.step(uh, 1)
+    with pytest.raises(_native.NonFiniteError, match="non-finite"):
+        p.check()
+    p.check()  # the flag was cleared by the report
+    lib = _native.load()
+    uh = _c64(spec)
+    p.step(uh, 2)
+    assert lib.l3es_plan_check(p._h) == 0
+    assert torch.isfinite(torch.view_as_real(uh)).all()
