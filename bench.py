@@ -43,21 +43,82 @@ CKP_N = 32
 WITH_PARTICLES = True  # coarsening + NUFFT + advection inside the step
 
 
+TRAFFIC_JSON = os.path.join(ROOT, "profiles", "dram_traffic_hit256.json")
+# kernel kinds of the library's timer -> name prefixes of their 256^3 launches in ncu
+TRAFFIC_KERNELS = {"line_cross": "line_cross<", "ky_pass_inv": "ky_inv_rhs<", "kx_inv_curl": "kx_inv_tma<256, 1, 1>",
+                   "rk_update": "k_rk_update<", "kx_fwd_band": "kx_fwd_band", "ky_pass_fwd": "ky_pass<256, (int)-1>"}
+
+
+def sources_sha256():
+    """Hash of the kernel sources (csrc/*.cu, *.cuh, *.h and the public header): a DRAM
+    traffic record applies only to the kernels it was measured on."""
+    import glob
+    import hashlib
+
+    h = hashlib.sha256()
+    files = []
+    for pat in ("ql-les-data_gb300/csrc/*.cu", "ql-les-data_gb300/csrc/*.cuh", "ql-les-data_gb300/csrc/*.h",
+                "include/*.h"):
+        files += glob.glob(os.path.join(ROOT, pat))
+    for f in sorted(files, key=lambda p: os.path.relpath(p, ROOT)):
+        h.update(os.path.relpath(f, ROOT).encode())
+        h.update(open(f, "rb").read())
+    return h.hexdigest()
+
+
+def record_traffic(csv_path, out_path, command):
+    """Turns an ncu launch list (`ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+    gpu__time_duration.sum --print-units base --csv --log-file CSV ...`) into a JSON
+    record of DRAM bytes per launch per kernel kind, tagged with the hash of the sources
+    it was measured on."""
+    import csv as _csv
+
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "nsecond": 1e-9, "usecond": 1e-6,
+             "msecond": 1e-3, "second": 1.0}
+    rows = [r for r in _csv.reader(open(csv_path)) if r]
+    head = next(i for i, r in enumerate(rows) if "Kernel Name" in r and "Metric Name" in r)
+    cols = rows[head]
+    ki, mi, ui, vi, ii = (cols.index(c) for c in ("Kernel Name", "Metric Name", "Metric Unit", "Metric Value", "ID"))
+    launches = {}
+    for r in rows[head + 1:]:
+        if len(r) <= vi:
+            continue
+        val = float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0)
+        launches.setdefault((r[ii], r[ki]), {})[r[mi]] = val
+    kinds = {}
+    for (_, name), m in launches.items():
+        kind = next((k for k, pre in TRAFFIC_KERNELS.items() if name.startswith(pre)), None)
+        if kind is None:
+            continue
+        d = kinds.setdefault(kind, {"kernel": name, "launches": 0, "dram_read_bytes": 0.0, "dram_write_bytes": 0.0,
+                                    "seconds": 0.0})
+        d["launches"] += 1
+        d["dram_read_bytes"] += m.get("dram__bytes_read.sum", 0.0)
+        d["dram_write_bytes"] += m.get("dram__bytes_write.sum", 0.0)
+        d["seconds"] += m.get("gpu__time_duration.sum", 0.0)
+    for d in kinds.values():
+        n = d["launches"]
+        d["traffic_per_launch"] = (d["dram_read_bytes"] + d["dram_write_bytes"]) / n
+        d["us_per_launch_serialised"] = 1e6 * d["seconds"] / n
+    rec = {"sources_sha256": sources_sha256(), "command": command, "kernels": kinds}
+    with open(out_path, "w") as f:
+        json.dump(rec, f, indent=1)
+    return rec
+
+
 def _ncu_traffic(kernel: str):
-    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu --set full
-    summary of the 256^3 stage (profiles/ncu_full_hit256_stage.md), or None."""
-    p = os.path.join(ROOT, "profiles", "ncu_full_hit256_stage.md")
-    if not os.path.exists(p):
-        return None
-    names = {"line_cross": "line_cross<256>", "ky_pass_inv": "ky_inv_rhs<256>", "kx_inv_curl": "kx_inv_tma<256, 1, 1>",
-             "rk_update": "k_rk_update<256, 3>", "kx_fwd_band": "kx_fwd_band_tma<256>",
-             "ky_pass_fwd": "ky_pass<256, (int)-1>"}
-    want = names.get(kernel)
-    for line in open(p):
-        cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if want and cells and cells[0] == want:
-            return (float(cells[2]) + float(cells[3])) * 1e6
-    return None
+    """(DRAM bytes read + written per launch of `kernel`, note) from the ncu record
+    profiles/dram_traffic_hit256.json, or (None, why) when there is none for these
+    kernel sources."""
+    if not os.path.exists(TRAFFIC_JSON):
+        return None, "no ncu traffic record"
+    rec = json.load(open(TRAFFIC_JSON))
+    if rec.get("sources_sha256") != sources_sha256():
+        return None, "the ncu traffic record was measured on other kernel sources"
+    d = rec.get("kernels", {}).get(kernel)
+    if not d:
+        return None, f"no {kernel} launches in the ncu traffic record"
+    return float(d["traffic_per_launch"]), "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch"
 
 
 def _peaks():
@@ -140,6 +201,18 @@ def initial_field(n):
     return u, float(dt)
 
 
+def initial_field_oracle(n):
+    """The same initial field from the FP64 oracle's restatement of init_fields.py
+    (used by the CPU arms, which import nothing from the product)."""
+    from oracle import numpy_ref as R
+
+    u = R.init_u_hit(n, SEED, spectrum="k4exp", kp=KP)
+    u *= np.sqrt(KE0 / (0.5 * np.mean(np.sum(u * u, axis=0))))
+    dx = 2 * np.pi / n
+    dt = CFL / (np.abs(u).max(axis=(1, 2, 3)) / dx + NU / dx**2).min()
+    return u, float(dt)
+
+
 def particles(c, seed=SEED):
     rng = np.random.default_rng(seed + 1)
     return rng.uniform(0.0, 2 * np.pi, size=(c**3, 3))
@@ -155,7 +228,7 @@ def cpu_step_rate(n, steps, warmup, u0=None, dt=None):
     cores = os.cpu_count() or 1
     R.set_workers(cores)
     if u0 is None:
-        u0, dt = initial_field(n)
+        u0, dt = initial_field_oracle(n)
     uh = R._rfftn(u0, axes=(1, 2, 3))
     mask = R.init_forcing_mask_hit(n, KF)
     step = R.rk4_wrapper(dt, R.rhs_wrapper(n, NU, const_power=(EPS_INJ, mask)), None, 0.0, "none")
@@ -246,6 +319,71 @@ def fp64_model(n, dt, nu=NU, kf=KF, eps_inj=EPS_INJ):
         return acc
 
     return rhs, step, wts
+
+
+def _spectral_stats(uh, n, nu=NU):
+    """FP64 statistics of a (3, n, n, n/2+1) half spectrum (either precision, promoted):
+    kinetic energy, shell energies E(s) over s = int(|k| + 0.5) (utils.py:35-97 up to its
+    constant factor, which cancels in a relative error) and the dissipation
+    nu <|curl u|^2> = nu sum w k^2 |u_hat|^2 / N^6 (utils.py:300-315), by Parseval."""
+    import torch
+
+    u = uh.to(torch.complex128)
+    dev = u.device
+    kx = torch.fft.fftfreq(n, 1.0 / n, dtype=torch.float64, device=dev)
+    kz = torch.arange(n // 2 + 1, dtype=torch.float64, device=dev)
+    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
+    w = torch.full((n // 2 + 1,), 2.0, dtype=torch.float64, device=dev)
+    w[0] = w[-1] = 1.0
+    e = (u.abs() ** 2).sum(0) * w / float(n) ** 6  # 2 x energy density per stored mode
+    shell = (k2.sqrt() + 0.5).long().flatten()
+    spec = torch.zeros(int(shell.max()) + 1, dtype=torch.float64, device=dev).index_add_(0, shell, e.flatten())
+    return {"ke": 0.5 * float(e.sum()), "spectrum": 0.5 * spec, "diss": nu * float((e * k2).sum())}
+
+
+def accuracy_check(plan, uh0, u0, dt, n, steps, marks=(100,)):
+    """The metric's accuracy clause and more: the FP32 step (this library) and the FP64
+    plain form (complex128 cuFFT, same GPU) from the same initial field, compared after
+    each of `marks` steps and after `steps`: relative kinetic-energy error (the criterion,
+    1e-5), shell-spectrum errors (maximum over the shells 1 <= s <= kd of
+    |E32 - E64| / E64, and the relative L2 error over those shells), the relative
+    dissipation error and the relative L2 error of the whole half spectrum. Also times
+    the FP64 comparator (CUDA events over its step loops only)."""
+    import torch
+
+    _, step64, _ = fp64_model(n, dt)
+    kd = int(np.floor(2.0 / 3.0 * (n // 2 + 1) - 1e-12))
+    uh32 = uh0.clone()
+    uh64 = torch.fft.rfftn(torch.from_numpy(u0).to("cuda"), dim=(1, 2, 3))
+    step64(uh64.clone())  # creates the cuFFT plans outside the timed loops (result discarded)
+    torch.cuda.synchronize()
+    ms64, done, out = 0.0, 0, []
+    for m in sorted(set([k for k in marks if 0 < k < steps] + [steps])):
+        plan.step(uh32, m - done)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(m - done):
+            uh64 = step64(uh64)
+        e1.record()
+        torch.cuda.synchronize()
+        ms64 += e0.elapsed_time(e1)
+        done = m
+        a, b = _spectral_stats(uh32, n), _spectral_stats(uh64, n)
+        sa, sb = a["spectrum"][1 : kd + 1], b["spectrum"][1 : kd + 1]
+        w = torch.full((n // 2 + 1,), 2.0, dtype=torch.float64, device="cuda")
+        w[0] = w[-1] = 1.0
+        d2 = float(((uh32.to(torch.complex128) - uh64).abs() ** 2 * w).sum())
+        out.append({"steps": m, "ke_fp32": a["ke"], "ke_fp64": b["ke"], "rel_err": abs(a["ke"] - b["ke"]) / b["ke"],
+                    "spectrum_max_rel_err": float(((sa - sb).abs() / sb).max()),
+                    "spectrum_l2_rel_err": float(torch.linalg.vector_norm(sa - sb) / torch.linalg.vector_norm(sb)),
+                    "dissipation_rel_err": abs(a["diss"] - b["diss"]) / b["diss"],
+                    "field_l2_rel_err": (d2 / float((uh64.abs() ** 2 * w).sum())) ** 0.5})
+    last = dict(out[-1])
+    last["criterion"] = 1e-5
+    last["shells"] = f"1..{kd}"
+    last["earlier"] = out[:-1]
+    del uh32, uh64
+    return last, 1e3 * steps / ms64
 
 
 def fp64_plain_rate(u0, dt, n, steps, warmup):
@@ -374,6 +512,118 @@ def run_adjoint(args):
             "adjoint": res}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ---------------------------------------------------------------------------------
+# further single-trajectory configurations (keys of the headline line)
+# ---------------------------------------------------------------------------------
+def jittered_lattice(c, dim, seed, jitter=0.25):
+    """c^dim particles on the cell centres of a c^dim lattice in [0, 2 pi)^dim, moved by
+    up to +-jitter cells (seeded), wrapped into the box."""
+    rng = np.random.default_rng(seed)
+    h = 2 * np.pi / c
+    ax = (np.arange(c) + 0.5) * h
+    g = np.stack([a.ravel() for a in np.meshgrid(*([ax] * dim), indexing="ij")], 1)
+    return np.mod(g + rng.uniform(-jitter, jitter, g.shape) * h, 2 * np.pi)
+
+
+def _graph_rate(record, steps, warmup):
+    """Steps/s of a step recorded as two ping-pong graphs (record(parity) -> Graph),
+    CUDA events on the current stream."""
+    import torch
+
+    graphs = [record(0), record(1)]
+    for i in range(max(warmup, 2)):
+        graphs[i & 1].launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        graphs[i & 1].launch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return 1e3 / ms, ms
+
+
+def hit_ekin_tot_rate(steps, warmup, n=N_GRID):
+    """The reference's own HIT configuration (configs/hit32_1.yaml: 256^3, nu = 2e-3,
+    dt = 2e-3, ekin_tot forcing on 0 < |k| <= 3 holding the kinetic energy at 1.25,
+    32^3 particles interpolated by NUFFT from the 32^3 coarsening and relaxed by SPH
+    with relax_dt_factor 2 and u_ref 4 every step, as combined.py:122-142, :199 runs
+    them). Initial field: init_u_hit's k^-5/3 spectrum, seed 42; particles: a jittered
+    lattice (the reference reads a relaxed particle file, which is not shipped)."""
+    import torch
+
+    from l3es import _native
+    from l3es import init_fields as F
+
+    nu, dt, kf, e0, c, u_ref, factor = 2e-3, 2e-3, 3, 1.25, 32, 4.0, 2.0
+    u = F.init_u_hit(n, 42)
+    u *= np.sqrt(e0 / (0.5 * np.mean(np.sum(u * u, axis=0))))
+    plan = _native.Plan(dim=3, n=n, nu=nu, dt=dt, forcing="ekin_tot", kf=kf, e_kin_init=e0)
+    uh = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
+    plan.rfftn(torch.from_numpy(u.astype(np.float32)).cuda(), uh)
+    npart = c**3
+    ip = _native.InterpPlan(dim=3, ckp_n=c, n_fine=n, width=6, np_max=npart)
+    sph = _native.SphPlan(3, c, 2 * np.pi, npart)
+    r = [torch.from_numpy(jittered_lattice(c, 3, 42)).cuda(), torch.empty(npart, 3, dtype=torch.float64, device="cuda")]
+    u_r, u_rel = (torch.empty(npart, 3, dtype=torch.float64, device="cuda") for _ in range(2))
+    einj = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def record(parity):
+        src, dst = (r[0], r[1]) if parity == 0 else (r[1], r[0])
+        cap = _native.Graph.begin()
+        plan.step(uh, 1, e_inj=einj, stream=cap)
+        ip.set_spectrum(uh, stream=cap)
+        ip.interp(src, u_r, backend="nufft", stream=cap)
+        sph.relax_velocity(src, u_r, u_rel, dt, factor, u_ref, r_out=dst, stream=cap)
+        return _native.Graph.end(cap)
+
+    rate, ms = _graph_rate(record, steps, warmup)
+    plan.check()
+    ke = torch.zeros(1, dtype=torch.float64, device="cuda")
+    plan.kinetic_energy(uh, ke)
+    return {"value": rate, "unit": "steps/s", "ms_per_step": ms, "steps": steps, "ke_after": float(ke),
+            "config": "reference configs/hit32_1.yaml: 256^3, nu 2e-3, dt 2e-3, ekin_tot kf=3 KE 1.25, "
+                      "32^3 particles (jittered lattice) by NUFFT w=6 + SPH relaxation (factor 2, u_ref 4), "
+                      "one graph launch per step"}
+
+
+def kolm2d_rate(steps, warmup, n=256):
+    """BASELINE's 2D Kolmogorov configuration: 256^2, f_x = sin(4 y), nu = 1e-3, linear
+    drag 0.1, random-phase initial field band-limited to |k| <= 8 with kinetic energy
+    0.5 (seed 0), dt = 1e-3; 64^2 particles on a jittered lattice interpolated by NUFFT
+    (sigma 2, width 6) from the 64^2 spectral coarsening and advected (Euler) every step."""
+    import torch
+
+    from l3es import _native
+    from l3es import init_fields as F
+
+    nu, dt, c = 1e-3, 1e-3, 64
+    u = F.init_u_random2d(n, 0, 8.0, 0.5)
+    plan = _native.Plan(dim=2, n=n, nu=nu, dt=dt, kolm_k=4, kolm_amp=1.0, drag=0.1)
+    uh = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
+    plan.rfftn(torch.from_numpy(u.astype(np.float32)).cuda(), uh)
+    npart = c * c
+    ip = _native.InterpPlan(dim=2, ckp_n=c, n_fine=n, width=6, np_max=npart)
+    r = [torch.from_numpy(jittered_lattice(c, 2, 0)).cuda(), torch.empty(npart, 2, dtype=torch.float64, device="cuda")]
+    u_r = torch.empty(npart, 2, dtype=torch.float64, device="cuda")
+
+    def record(parity):
+        src, dst = (r[0], r[1]) if parity == 0 else (r[1], r[0])
+        cap = _native.Graph.begin()
+        plan.step(uh, 1, stream=cap)
+        ip.set_spectrum(uh, stream=cap)
+        ip.interp(src, u_r, backend="nufft", dt=dt, r_out=dst, stream=cap)
+        return _native.Graph.end(cap)
+
+    k = max(steps, 1000)
+    rate, ms = _graph_rate(record, k, warmup)
+    plan.check()
+    return {"value": rate, "unit": "steps/s", "ms_per_step": ms, "steps": k,
+            "config": "2D Kolmogorov 256^2, sin(4y) forcing, nu 1e-3, drag 0.1, random2d |k|<=8 KE 0.5, dt 1e-3, "
+                      "64^2 jittered particles by NUFFT w=6 from the 64^2 coarsening, Euler; one graph launch per step"}
 
 
 # ---------------------------------------------------------------------------------
@@ -563,19 +813,21 @@ def run_ours(args):
     ke_check = None
     fp64_rate = None
     if rank == 0 and not args.skip_baselines and args.ke_steps > 0:
-        uh_chk = uh0.clone()
-        plan.step(uh_chk, args.ke_steps)
-        ke_dev2 = torch.zeros(1, dtype=torch.float64, device="cuda")
-        plan.kinetic_energy(uh_chk, ke_dev2)
-        ke32 = float(ke_dev2)
-        fp64_rate, ke64 = fp64_plain_rate(u0, dt, n, steps=args.ke_steps, warmup=0)
-        ke_check = {"steps": args.ke_steps, "ke_fp32": ke32, "ke_fp64": ke64,
-                    "rel_err": abs(ke32 - ke64) / ke64, "criterion": 1e-5}
-        del uh_chk
+        ke_check, fp64_rate = accuracy_check(plan, uh0, u0, dt, n, args.ke_steps, marks=(100,))
+        plan.check()  # no blow-up and no bounded wait gave up over the K steps
 
     adjoint = None
     if rank == 0 and not args.skip_baselines and args.adjoint_dirs > 0:
         adjoint = adjoint_check(dirs=args.adjoint_dirs)
+    extra = {}
+    if rank == 0 and not args.skip_baselines:
+        extra["hit_ekin_tot"] = hit_ekin_tot_rate(args.steps, args.warmup)
+        extra["kolm2d_256"] = kolm2d_rate(args.steps, args.warmup)
+        b = run_batch24(args, emit=False)
+        extra["batch24"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "steps", "speedup_vs_sequential",
+                                              "sequential")}
+        extra["batch24"]["workload"] = b["config"]["workload"]
+        extra["batch24"]["batched"] = b["config"]["batched"]
 
     line = None
     if rank == 0 and args.skip_baselines:
@@ -586,6 +838,7 @@ def run_ours(args):
         if fp64_rate is None:
             fp64_rate, _ = fp64_plain_rate(u0, dt, n, steps=max(2, min(args.steps, 5)), warmup=1)
         cpu_rate, cores = cpu_step_rate(n, 1, 0, u0=u0, dt=dt)
+        traffic, traffic_note = _ncu_traffic(name)
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -596,8 +849,9 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "1 gpu",
                        "l2": "working set (~1.3 GB) larger than L2, no flush"},
             "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": _ncu_traffic(name),
-                         "algo_bytes_per_launch": tb / nl, "ms_per_launch": tms / nl},
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "traffic_source": traffic_note, "algo_bytes_per_launch": tb / nl,
+                         "ms_per_launch": tms / nl},
             "kernels": kernels,
             "fp64_plain": {"value": fp64_rate, "unit": "steps/s", "speedup": value / world / fp64_rate,
                            "note": "reference algorithm restated with torch.fft (cuFFT) in complex128, same GPU"},
@@ -612,6 +866,7 @@ def run_ours(args):
                             "value: the host reads step i's results while step i+1 runs (double-buffered pinned "
                             "outputs); synced_each_step: the host waits for every step before the next"},
             "with_u_out": with_u_out,
+            **extra,
             "gpu_launches": launches,
             "clocks": clocks,
             "workspace_gb": plan.workspace_bytes / 1e9,
@@ -659,7 +914,8 @@ def _batch_runs():
     return runs
 
 
-def run_batch24(args):
+def run_batch24(args, emit=True):
+    """Times the 24-trajectory workload; prints its JSON line (emit) or returns it."""
     import torch
 
     from l3es import _native
@@ -770,6 +1026,8 @@ def run_batch24(args):
         "speedup_vs_sequential": batched_rate / seq_rate,
         "clocks": clk.summary(),
     }
+    if not emit:
+        return line
     print(json.dumps(line), flush=True)
     return 0
 
@@ -785,13 +1043,23 @@ def main():
                     help="hit256: the metric's 256^3 step; batch24: 24 mixed trajectories; "
                          "adjoint: the 128^3 differentiation workload alone")
     ap.add_argument("--batch-steps", type=int, default=500)
-    ap.add_argument("--ke-steps", type=int, default=200,
-                    help="steps of the FP32-vs-FP64 kinetic energy check (0 = skip)")
+    ap.add_argument("--ke-steps", type=int, default=1000,
+                    help="steps of the FP32-vs-FP64 accuracy check: kinetic energy (the metric's clause), "
+                         "spectrum, dissipation and field errors (0 = skip)")
     ap.add_argument("--adjoint-dirs", type=int, default=16,
                     help="directions of the 128^3 adjoint finite-difference check (0 = skip the adjoint leg)")
     ap.add_argument("--skip-baselines", action="store_true",
                     help="profiling runs: time our step only (no FP64 plain, CPU or e2e legs)")
+    ap.add_argument("--record-traffic", metavar="NCU_CSV", default=None,
+                    help="no benchmark: turn an ncu DRAM launch list of the 256^3 step into the JSON traffic record "
+                         "(--traffic-out) that the headline's roofline.traffic reads")
+    ap.add_argument("--traffic-out", default=TRAFFIC_JSON)
+    ap.add_argument("--traffic-command", default="", help="the ncu command that made NCU_CSV (stored in the record)")
     args = ap.parse_args()
+    if args.record_traffic:
+        rec = record_traffic(args.record_traffic, args.traffic_out, args.traffic_command)
+        print(json.dumps({k: v["traffic_per_launch"] for k, v in rec["kernels"].items()}))
+        return 0
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
