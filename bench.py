@@ -86,7 +86,10 @@ def record_traffic(csv_path, out_path, command):
         val = float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0)
         launches.setdefault((r[ii], r[ki]), {})[r[mi]] = val
     kinds = {}
-    for (_, name), m in launches.items():
+    for (_, full), m in launches.items():
+        # "void line_cross2<256>(const float2 *, ...)" -> "line_cross2<256>"
+        name = full[5:] if full.startswith("void ") else full
+        name = name.split("(")[0].replace("l3es::", "")
         kind = next((k for k, pre in TRAFFIC_KERNELS.items() if name.startswith(pre)), None)
         if kind is None:
             continue

@@ -58,7 +58,16 @@ typedef struct l3es_plan_desc {
   double eps_inj;     /* extension: constant-power injection rate */
   double drag;        /* extension: linear drag coefficient */
   double kolm_amp;    /* extension: Kolmogorov forcing amplitude */
+  int32_t scheme;     /* L3ES_SCHEME_*: how the step treats the viscous term */
 } l3es_plan_desc;
+
+/* The reference's explicit RK4 (du -= nu k^2 u_hat, l3es/spectral_solver.py:59). */
+#define L3ES_SCHEME_EXPLICIT 0
+/* Extension: RK4 with the viscous term integrated exactly by the factor
+ * exp(-nu k^2 t) (Lawson's integrating-factor RK4); fourth-order like the explicit
+ * form, and stable for any nu k^2 dt. l3es_rhs still returns the full right-hand side;
+ * the adjoint calls refuse plans with this scheme. */
+#define L3ES_SCHEME_INTEGRATING_FACTOR 1
 
 /* Builds the closures' constant state of rhs_wrapper / rk4_wrapper
  * (l3es/spectral_solver.py:27-48, :65-71): twiddle tables, dealias band, scratch. */
@@ -186,6 +195,15 @@ int l3es_interp_coarse_spectrum(l3es_interp_plan* plan, void* out, void* stream)
  * r_out (nullable): shift_fn(r, dt * u_r) (integrator.py:21-23, combined.py:199). */
 int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r,
                 int32_t backend, double dt, double* r_out, void* stream);
+
+/* Extension: particle advection by classical RK4 instead of the reference's explicit
+ * Euler step (shift_fn(r, dt * u_r), integrator.py:21-23, combined.py:199), through the
+ * plan's current coarse field held fixed over the step: four interpolations (backend as
+ * in l3es_interp) at r, r + dt/2 v1, r + dt/2 v2, r + dt v3 (stage positions wrapped
+ * into the box), r_out = (r + dt/6 (v1 + 2 v2 + 2 v3 + v4)) mod 2 pi. u_r receives v1,
+ * the velocity at r (what l3es_interp returns). r, u_r and r_out must be separate. */
+int l3es_interp_advect_rk4(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r,
+                           int32_t backend, double dt, double* r_out, void* stream);
 
 /* Allocation-free form of l3es_interp_set_spectrum + l3es_interp(backend dft): no
  * counterpart in the reference. For hosts that cannot let a library allocate

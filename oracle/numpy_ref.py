@@ -196,6 +196,40 @@ def rk4_wrapper(dt, rhs_fn, forcing_mask, e_kin_init, forcing_type,
     return step_fn
 
 
+def rk4_if_wrapper(dt, rhs_fn_inviscid, nu, N, fft_axes=(1, 2, 3)):
+    """Extension (no reference counterpart): the classical RK4 step with the viscous term
+    integrated exactly by an integrating factor (Lawson's RK4 on v = exp(nu k^2 t) u_hat).
+    rhs_fn_inviscid is rhs_wrapper(N, 0.0, ...) (the right-hand side without viscosity);
+    with E(s) = exp(-nu k^2 s):
+        k1 = R(u0);  a = E(h/2) (u0 + h/2 k1)
+        k2 = R(a);   b = E(h/2) u0 + h/2 k2
+        k3 = R(b);   c = E(h) u0 + h E(h/2) k3
+        k4 = R(c);   u1 = E(h) u0 + h/6 (E(h) k1 + 2 E(h/2) (k2 + k3) + k4)
+    Returns step_fn(u, u_hat) -> (u, u_hat, 0.0) like rk4_wrapper."""
+    dim = len(fft_axes)
+    _, kkk2, _, _ = wavenumbers(N, dim)
+    eh = np.exp(-nu * kkk2 * 0.5 * dt)
+    e1 = eh * eh
+    h = dt
+
+    def step_fn(u, u_hat):
+        u0 = u_hat
+        k1 = rhs_fn_inviscid(u, u0, 0)
+        a = eh * (u0 + 0.5 * h * k1)
+        k2 = rhs_fn_inviscid(None, a, 1)
+        b = eh * u0 + 0.5 * h * k2
+        k3 = rhs_fn_inviscid(None, b, 2)
+        c = e1 * u0 + h * eh * k3
+        k4 = rhs_fn_inviscid(None, c, 3)
+        u1 = e1 * u0 + h / 6.0 * (e1 * k1 + 2.0 * eh * (k2 + k3) + k4)
+        u_new = _irfftn(u1, axes=fft_axes)
+        if dim == 2:
+            u_new = np.expand_dims(u_new, -1)
+        return u_new, u1, 0.0
+
+    return step_fn
+
+
 def comp_dt(u, dx, nu, cfl=1.0):
     """spectral_solver.py:123-127 (Hickel et al. 2006, eq. 61)."""
     umax = np.max(np.abs(u), axis=(1, 2, 3))
@@ -507,6 +541,21 @@ def interpolate_dft(u, r, chunk=2048):
             val = np.einsum("cpa,pa->cp", t, ex)
         out[s : s + chunk] = (val.real / c**dim).T
     return out
+
+
+def advect_rk4(interp, r, dt, box_size=2 * np.pi):
+    """Extension (no reference counterpart; the reference advances particles by one
+    explicit Euler step with the post-step velocity, integrator.py:21-23 and
+    combined.py:199): classical RK4 for dr/dt = u(r) with the velocity field held fixed
+    at the post-step field. interp(r) -> velocities (Np, dim). Returns (u(r), r_new):
+        v1 = u(r),  v2 = u(r + dt/2 v1),  v3 = u(r + dt/2 v2),  v4 = u(r + dt v3),
+        r_new = (r + dt/6 (v1 + 2 v2 + 2 v3 + v4)) mod box
+    (stage positions wrapped into the box as well)."""
+    v1 = interp(r)
+    v2 = interp(np.mod(r + 0.5 * dt * v1, box_size))
+    v3 = interp(np.mod(r + 0.5 * dt * v2, box_size))
+    v4 = interp(np.mod(r + dt * v3, box_size))
+    return v1, np.mod(r + dt / 6.0 * (v1 + 2.0 * v2 + 2.0 * v3 + v4), box_size)
 
 
 def interpolate_from_uhat_dft(u_hat, N, ckp_N, r, dim=3):

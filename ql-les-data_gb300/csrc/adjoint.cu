@@ -53,6 +53,9 @@ static int adj_check(l3es_plan* p, const char* who) {
     return fail(L3ES_EINVAL, std::string(who) +
                                  ": the ekin_tot rescaling after each step has no adjoint here "
                                  "(use forcing none or const_power)");
+  if (p->desc.scheme != L3ES_SCHEME_EXPLICIT)
+    return fail(L3ES_EINVAL, std::string(who) + ": the adjoint follows the explicit RK4 step only "
+                                                "(L3ES_SCHEME_EXPLICIT)");
   return adj_prepare(p);
 }
 
@@ -114,6 +117,7 @@ int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* str
     prm.kolm_k = d.kolm_k;
     prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
     prm.rk = rk;
+    prm.if_h = 0.f;
     plan->tab.stage(c, rk == 0 ? U0 : stage_out[rk - 1], U0, stage_out[rk], rk, prm, s);
   }
   const float dt = (float)d.dt;

@@ -473,6 +473,156 @@ line_cross(const float2* __restrict__ w, long long fs, float2* __restrict__ du, 
 }
 
 // ------------------------------------------------------------------------------
+// Half-axis line pass of the RHS, two real lines per complex FFT (N = 64 .. 256).
+//
+// Two real lines x, y of length N have spectra X, Y (half axis, H = N/2 + 1 values);
+// one N-point complex inverse FFT of Z = X_ext + i Y_ext (Hermitian extensions) gives
+// x + i y, and one forward FFT of x + i y gives Z with X[k] = (Z[k] + conj Z[N-k]) / 2,
+// Y[k] = (Z[k] - conj Z[N-k]) / (2 i). A line's six fields pair up as (u_x, u_y),
+// (u_z, curl_x), (curl_y, curl_z): after three inverse FFTs every lane holds all six
+// physical values at its own N/T positions, so u x curl u is formed in registers (no
+// parking in shared memory). Its x, y components pair in one forward FFT; the z
+// component waits for the z component of the next line, and the two share one. A line
+// takes T = N/8 lanes (N = 256: a whole warp); a line slot does two lines (A then B),
+// lines counted from the last (as in line_cross). Per pair of lines: 9 N-point FFTs
+// against 18 N/2-point FFTs with pack / unpack passes and parked velocities.
+// ct: compact twiddle table of the N-point FFT (Sched<N, 8>, at line2_ct_offset<N>()
+// in the plan's table).
+// ------------------------------------------------------------------------------
+template <int N>
+__host__ __device__ constexpr int line2_ct_offset() {
+  return N + Sched<N / 2, Fft<N / 2>::E>::ctlen();
+}
+
+// Z[n] = X_ext[n] + i Y_ext[n] for n = t + T e (lane t, slot e) from two half-spectrum
+// lines (numpy irfft semantics: the imaginary parts of X[0] and X[N/2] are ignored).
+template <int N>
+__device__ __forceinline__ void c2r_pair_load(const float2* __restrict__ X, const float2* __restrict__ Y, int t,
+                                              float2 (&z)[8]) {
+  constexpr int T = N / 8;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int n = t + T * e;
+    const bool lo = e < 4;  // n < N/2 (e = 4 starts at the Nyquist entry N/2 + 0)
+    const int idx = lo ? n : N - n;
+    float2 x = __ldg(X + idx), y = __ldg(Y + idx);
+    if ((e == 0 || e == 4) && t == 0) {  // n = 0 and n = N/2: real parts only
+      x.y = 0.f;
+      y.y = 0.f;
+    }
+    z[e] = lo ? make_float2(x.x - y.y, x.y + y.x)   // X + i Y
+              : make_float2(x.x + y.y, y.x - x.y);  // conj X + i conj Y (mirror N - n)
+  }
+}
+
+// From Z = FFT(x + i y) in registers (lane t, slot e holds Z[t + T e]): X[k] and Y[k] for
+// k = t + T e, e < 4, scaled by s (s includes the 1/2).
+template <int N>
+__device__ __forceinline__ void r2c_pair_unpack(const float2 (&z)[8], int t, float s, float2 (&X)[4],
+                                                float2 (&Y)[4]) {
+  constexpr int T = N / 8;
+  const int lane = threadIdx.x & 31;
+  const int src = lane - t + (t == 0 ? 0 : T - t);  // lane holding Z[N - k]
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    // the partner Z[N - k] is slot 7 - e of lane T - t, or slot (8 - e) mod 8 of lane 0
+    const float2 give = (t == 0) ? z[(8 - e) & 7] : z[7 - e];
+    float2 zm;
+    zm.x = __shfl_sync(0xffffffffu, give.x, src);
+    zm.y = __shfl_sync(0xffffffffu, give.y, src);
+    const float2 zk = z[e];
+    X[e] = make_float2(s * (zk.x + zm.x), s * (zk.y - zm.y));
+    Y[e] = make_float2(s * (zk.y + zm.y), s * (zm.x - zk.x));
+  }
+}
+
+// stores X[k], k = t + T e < kt, of one DU line (zeros for kd < k < kt)
+template <int N>
+__device__ __forceinline__ void store_du_line(float2* __restrict__ dst, const float2 (&X)[4], int t, int kt, int kd) {
+  constexpr int T = N / 8;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int k = t + T * e;
+    if (k < kt) dst[k] = k <= kd ? X[e] : make_float2(0.f, 0.f);
+  }
+}
+
+template <int N>
+struct Line2Cfg {
+  static constexpr int T = N / 8;             // lanes per line
+  static constexpr int THREADS = 128;
+  static constexpr int SLOTS = THREADS / T;   // line slots per CTA
+  static constexpr int LPC = 2 * SLOTS;       // lines per CTA (two per slot)
+  static constexpr int XS = xpad_len<1>(N);   // exchange slots per line slot
+};
+
+template <int N>
+__global__ void __launch_bounds__(Line2Cfg<N>::THREADS, 4)
+line_cross2(const float2* __restrict__ w, long long fs, float2* __restrict__ du, long long ds, int kt, int kd,
+            float s2, const float2* __restrict__ ct, int nlines) {
+  static_assert(N >= 64 && N <= 256, "two-for-one line pass: N in [64, 256]");
+  using C = Line2Cfg<N>;
+  constexpr int T = C::T, H = N / 2 + 1;
+  __shared__ float2 s_x[C::SLOTS * C::XS];
+  const int slot = threadIdx.x / T, t = threadIdx.x % T;
+  float2* xs = s_x + slot * C::XS;
+  const float2* wb = w + (long long)blockIdx.y * 6 * fs;
+  float2* db = du + (long long)blockIdx.y * 3 * ds;
+  const long long ia = 2 * ((long long)blockIdx.x * C::SLOTS + slot);  // line A; B = A + 1
+  float pa[8], pb[8];  // z component of u x curl u of lines A and B
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const long long idx = ia + half;
+    const bool valid = idx < nlines;
+    const long long line = valid ? nlines - 1 - idx : nlines - 1;  // idle slots mirror a valid line
+    const float2* src = wb + line * H;
+    float2 h1[8], h2[8], z[8];
+    c2r_pair_load<N>(src, src + fs, t, z);  // u_x + i u_y
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) h1[e] = z[e];
+    __syncwarp();
+    c2r_pair_load<N>(src + 2 * fs, src + 3 * fs, t, z);  // u_z + i curl_x
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) h2[e] = z[e];
+    __syncwarp();
+    c2r_pair_load<N>(src + 4 * fs, src + 5 * fs, t, z);  // curl_y + i curl_z
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
+    __syncwarp();
+    // u x curl u at this lane's positions (unnormalised: the scale enters in s2)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const float ux = h1[e].x, uy = h1[e].y, uz = h2[e].x, wx = h2[e].y, wy = z[e].x, wz = z[e].y;
+      const float pz = fmaf(ux, wy, -uy * wx);
+      if (half == 0)
+        pa[e] = pz;
+      else
+        pb[e] = pz;
+      z[e] = make_float2(fmaf(uy, wz, -uz * wy), fmaf(uz, wx, -ux * wz));
+    }
+    warp_fft<N, 8, kFwd>(z, xs, t, ct);
+    float2 X[4], Y[4];
+    r2c_pair_unpack<N>(z, t, s2, X, Y);
+    if (valid) {
+      float2* dst = db + line * kt;
+      store_du_line<N>(dst, X, t, kt, kd);
+      store_du_line<N>(dst + ds, Y, t, kt, kd);
+    }
+    __syncwarp();
+  }
+  // z components of lines A and B in one forward FFT
+  float2 z[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) z[e] = make_float2(pa[e], pb[e]);
+  warp_fft<N, 8, kFwd>(z, xs, t, ct);
+  float2 X[4], Y[4];
+  r2c_pair_unpack<N>(z, t, s2, X, Y);
+  if (ia < nlines) store_du_line<N>(db + 2 * ds + (nlines - 1 - ia) * kt, X, t, kt, kd);
+  if (ia + 1 < nlines) store_du_line<N>(db + 2 * ds + (nlines - 2 - ia) * kt, Y, t, kt, kd);
+}
+
+// ------------------------------------------------------------------------------
 // Half-axis c2r of 3 fields to physical space (irfftn's last axis): out[c][line][0..N).
 // ------------------------------------------------------------------------------
 template <int N>
@@ -640,6 +790,7 @@ struct EpiParams {
   int kolm_k;        //   (2D extension, kolm_k = 0 = off)
   int band_kf2;      // constant-power band forcing 0 < |k|^2 <= band_kf2 (0 = off)
   int rk;            // 0..3, or -1: write the right-hand side du itself to `out`
+  float if_h;        // > 0: integrating-factor RK4 with step if_h (viscous term exact)
 };
 
 // Float-float (hi + lo) accumulator: error-free FP32 additions (Knuth's TwoSum, then
@@ -869,8 +1020,11 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
     const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
     r = __ldg(P + c * pcs + row * kt + kh);
   }
-  r.x -= nu * kk2 * sv.x;
-  r.y -= nu * kk2 * sv.y;
+  const bool vif = prm.if_h > 0.f && prm.rk >= 0;
+  if (!vif) {
+    r.x -= nu * kk2 * sv.x;
+    r.y -= nu * kk2 * sv.y;
+  }
   if (prm.drag != 0.f) {
     r.x -= prm.drag * sv.x;
     r.y -= prm.drag * sv.y;
@@ -883,6 +1037,33 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
   if (prm.rk < 0) {
     nv = r;
     return r;
+  }
+  if (vif) {
+    // Integrating-factor RK4 (Lawson) with eh = exp(-nu k^2 h / 2), e1 = eh^2 and r the
+    // right-hand side without viscosity:
+    //   rk 0: out = eh (u0 + h/2 r)                         (us = u0; no accumulator)
+    //   rk 1: out = eh u0 + h/2 r,  acc = 2/3 e1 u0 + eh/3 us + h/3 eh r
+    //         (h/6 e1 k1 rebuilt from us = eh (u0 + h/2 k1), as in the explicit form)
+    //   rk 2: out = e1 u0 + h eh r, acc += h/3 eh r
+    //   rk 3: fin = acc + h/6 r
+    const float eh = expf(-0.5f * prm.if_h * nu * kk2);
+    const float e1 = eh * eh;
+    if (prm.rk == 0) {
+      nv = make_float2(eh * fmaf(prm.b_dt, r.x, sv.x), eh * fmaf(prm.b_dt, r.y, sv.y));
+      return r;
+    }
+    if (prm.rk == 1) {
+      nv = make_float2(fmaf(eh, z0.x, prm.b_dt * r.x), fmaf(eh, z0.y, prm.b_dt * r.y));
+      const float c0 = (2.0f / 3.0f) * e1, c1 = eh * (1.0f / 3.0f), c2 = prm.a_dt * eh;
+      return make_float2(fmaf(c2, r.x, fmaf(c1, sv.x, c0 * z0.x)), fmaf(c2, r.y, fmaf(c1, sv.y, c0 * z0.y)));
+    }
+    if (prm.rk == 2) {
+      const float bh = prm.b_dt * eh, ah = prm.a_dt * eh;
+      nv = make_float2(fmaf(bh, r.x, e1 * z0.x), fmaf(bh, r.y, e1 * z0.y));
+      return make_float2(fmaf(ah, r.x, a0.x), fmaf(ah, r.y, a0.y));
+    }
+    nv = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
+    return nv;
   }
   if (prm.rk == 0) {  // the accumulator is not stored: stage 1 rebuilds it from us and u0
     nv = make_float2(fmaf(prm.b_dt, r.x, sv.x), fmaf(prm.b_dt, r.y, sv.y));

@@ -84,9 +84,17 @@ struct DnsOps {
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
                   ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
-    L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
-                line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
-                    c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));
+    if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT
+      using L2 = Line2Cfg<N>;
+      const float s2 = 0.5f * scale * scale;
+      L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                  line_cross2<N><<<dim3((unsigned)((lines + L2::LPC - 1) / L2::LPC), c.batch), L2::THREADS, 0, s>>>(
+                      c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines));
+    } else {
+      L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                  line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
+                      c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));
+    }
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_FWD, Adu * (1.0 + rows), s,
                   ky_pass<N, kFwd><<<dim3(ky_tiles(c.kt), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd,

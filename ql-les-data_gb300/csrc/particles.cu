@@ -322,6 +322,36 @@ k_p2g_dft(const double* __restrict__ r, const double* __restrict__ u_r, long lon
     for (int c = 0; c < 3; ++c) S[c * scs + m] = make_float2((float)acc[c][0], (float)acc[c][1]);
 }
 
+// Stages of classical RK4 particle advection through a field held fixed (extension),
+// elementwise over the n = np * dim coordinates; v: the velocity at the stage positions.
+//   stage 0: acc = v,    rs = wrap(r0 + dt/2 v)
+//   stage 1: acc += 2 v, rs = wrap(r0 + dt/2 v)
+//   stage 2: acc += 2 v, rs = wrap(r0 + dt v)
+//   stage 3: rs = wrap(r0 + dt/6 (acc + v))          (rs = the caller's r_out)
+__global__ void k_rk4_particles(int stage, const double* __restrict__ r0, const double* __restrict__ v,
+                                double* __restrict__ acc, double* __restrict__ rs, double dt, long long n,
+                                double box) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double vi = v[i];
+  double x;
+  if (stage == 0) {
+    acc[i] = vi;
+    x = r0[i] + 0.5 * dt * vi;
+  } else if (stage == 1) {
+    acc[i] += 2.0 * vi;
+    x = r0[i] + 0.5 * dt * vi;
+  } else if (stage == 2) {
+    acc[i] += 2.0 * vi;
+    x = r0[i] + dt * vi;
+  } else {
+    x = r0[i] + dt / 6.0 * (acc[i] + vi);
+  }
+  x = x - box * floor(x / box);
+  if (x >= box) x -= box;
+  rs[i] = x;
+}
+
 // shift_fn(r, dr) = (r + scale * dr) mod box (integrator.py:21-23), elementwise
 __global__ void k_shift(const double* __restrict__ r, const double* __restrict__ dr, long long n, double scale,
                         double box, double* __restrict__ out) {
@@ -454,6 +484,9 @@ struct l3es_interp_plan {
   int* start = nullptr;      // [nb^dim]
   int* perm = nullptr;       // [np_max]
   double* red = nullptr;     // [1024] loss partial sums
+  double* rk_acc = nullptr;  // [np_max][dim] RK4 advection: velocity accumulator
+  double* rk_pos = nullptr;  // [np_max][dim]   stage positions
+  double* rk_vel = nullptr;  // [np_max][dim]   stage velocities
   l3es_plan* coarse = nullptr;  // size-c transforms (irfftn of Hh, rfftn of a coarse field)
   long long hcs = 0, gcs = 0;
   Ctx gctx;                  // geometry for the grid passes (twiddles only)
@@ -563,6 +596,10 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * nbins, "bin starts");
   rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * (np_max > 0 ? np_max : 1), "permutation");
   rc = rc ? rc : ip_alloc(p, (void**)&p->red, sizeof(double) * 1024, "loss partials");
+  const size_t rk_bytes = sizeof(double) * dim * (np_max > 0 ? np_max : 1);
+  rc = rc ? rc : ip_alloc(p, (void**)&p->rk_acc, rk_bytes, "rk4 accumulator");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->rk_pos, rk_bytes, "rk4 stage positions");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->rk_vel, rk_bytes, "rk4 stage velocities");
   if (rc == L3ES_OK) {
     l3es_plan_desc d{};
     d.dim = dim;
@@ -653,6 +690,52 @@ int l3es_interp_coarse_spectrum(l3es_interp_plan* p, void* out, void* stream) {
                     "l3es_interp_coarse_spectrum");
 }
 
+}  // extern "C"
+
+// Exact interpolation (dft backend) at r into u_r, with the fused Euler shift when r_out.
+static int dft_eval(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, double dt, double* r_out,
+                    cudaStream_t s) {
+  const int ncomp = p->dim;
+  const unsigned pb = (unsigned)((np + 127) / 128);
+  const size_t smem = sizeof(float2) * p->dim * p->c * 128;
+  if (p->dim == 3) {
+    cudaFuncSetAttribute(k_dft_interp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_dft_interp<3><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
+  } else {
+    cudaFuncSetAttribute(k_dft_interp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_dft_interp<2><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
+  }
+  return cuda_check(cudaGetLastError(), "l3es_interp (dft) launch");
+}
+
+// NUFFT gather at r from the prepared fine grid (nufft_grid), visiting particles in the
+// bin order of the positions nufft_grid was given; fused Euler shift when r_out.
+static int nufft_eval(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, double dt, double* r_out,
+                      cudaStream_t s) {
+  const int ncomp = p->dim;
+  const double norm = 1.0 / (std::pow((double)p->n, p->dim) * std::pow((double)p->c, p->dim));
+  const float beta = (float)p->beta;
+  const unsigned gblk = (unsigned)((np * kGatherLanes + 127) / 128);
+#define L3ES_GATHER(D, W)                                                                                   \
+  k_nufft_gather<D, W><<<gblk, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
+                                          r_out)
+  if (p->dim == 3) {
+    if (p->w == 6) L3ES_GATHER(3, 6);
+    else if (p->w == 8) L3ES_GATHER(3, 8);
+    else L3ES_GATHER(3, 4);
+  } else {
+    if (p->w == 6) L3ES_GATHER(2, 6);
+    else if (p->w == 8) L3ES_GATHER(2, 8);
+    else L3ES_GATHER(2, 4);
+  }
+#undef L3ES_GATHER
+  return cuda_check(cudaGetLastError(), "l3es_interp launch");
+}
+
+static int nufft_grid(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s);
+
+extern "C" {
+
 int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, int32_t backend, double dt,
                 double* r_out, void* stream) {
   if (!p || !r || !u_r) return fail(L3ES_EINVAL, "l3es_interp: null argument");
@@ -660,19 +743,42 @@ int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, i
   if (backend != 0 && backend != 1) return fail(L3ES_EINVAL, "l3es_interp: backend must be 0 (nufft) or 1 (dft)");
   if (np == 0) return L3ES_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  const int ncomp = p->dim;  // 3D: 3 velocity components; 2D: u, v (combined.py:122)
-  const unsigned pb = (unsigned)((np + 127) / 128);
-  if (backend == 1) {
-    const size_t smem = sizeof(float2) * p->dim * p->c * 128;
-    if (p->dim == 3) {
-      cudaFuncSetAttribute(k_dft_interp<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dft_interp<3><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
-    } else {
-      cudaFuncSetAttribute(k_dft_interp<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dft_interp<2><<<pb, 128, smem, s>>>(p->hh, p->hcs, p->c, ncomp, r, np, u_r, dt, r_out);
-    }
-    return cuda_check(cudaGetLastError(), "l3es_interp (dft) launch");
+  if (backend == 1) return dft_eval(p, r, np, u_r, dt, r_out, s);
+  const int rc = nufft_grid(p, r, np, s);
+  return rc != L3ES_OK ? rc : nufft_eval(p, r, np, u_r, dt, r_out, s);
+}
+
+int l3es_interp_advect_rk4(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, int32_t backend,
+                           double dt, double* r_out, void* stream) {
+  if (!p || !r || !u_r || !r_out) return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: null argument");
+  if (np < 0 || np > p->np_max) return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: np outside [0, np_max]");
+  if (backend != 0 && backend != 1)
+    return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: backend must be 0 (nufft) or 1 (dft)");
+  if (r_out == r || u_r == r || u_r == r_out)
+    return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: r, u_r and r_out must be separate arrays");
+  if (np == 0) return L3ES_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = backend == 0 ? nufft_grid(p, r, np, s) : L3ES_OK;  // one grid, bins of r reused by every stage
+  const long long n = np * p->dim;
+  const unsigned eb = (unsigned)((n + 255) / 256);
+  const double box = 2.0 * 3.14159265358979323846;
+  for (int stage = 0; stage < 4 && rc == L3ES_OK; ++stage) {
+    const double* pos = stage == 0 ? r : p->rk_pos;
+    double* vel = stage == 0 ? u_r : p->rk_vel;  // u_r: the velocity at the old positions
+    rc = backend == 0 ? nufft_eval(p, pos, np, vel, 0.0, nullptr, s) : dft_eval(p, pos, np, vel, 0.0, nullptr, s);
+    if (rc != L3ES_OK) break;
+    k_rk4_particles<<<eb, 256, 0, s>>>(stage, r, vel, p->rk_acc, stage == 3 ? r_out : p->rk_pos, dt, n, box);
+    rc = cuda_check(cudaGetLastError(), "l3es_interp_advect_rk4 launch");
   }
+  return rc;
+}
+
+}  // extern "C"
+
+// Fine NUFFT grid of the plan's coarse spectrum (deconvolve, zero-pad, 3 c2c passes, Re)
+// and the bin order of the positions r.
+static int nufft_grid(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s) {
+  const unsigned pb = (unsigned)((np + 127) / 128);
   const unsigned gb = (unsigned)((p->gcs + 255) / 256);
   if (p->dim == 3)
     k_nufft_prep<3><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
@@ -692,24 +798,10 @@ int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, i
     k_bin_scan<<<1, 1024, 0, s>>>(p->count, nbins, p->start);
     k_bin_scatter<2><<<pb, 128, 0, s>>>(r, np, p->nb, p->start, p->perm);
   }
-  const double norm = 1.0 / (std::pow((double)p->n, p->dim) * std::pow((double)p->c, p->dim));
-  const float beta = (float)p->beta;
-  const unsigned gblk = (unsigned)((np * kGatherLanes + 127) / 128);
-#define L3ES_GATHER(D, W)                                                                                   \
-  k_nufft_gather<D, W><<<gblk, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
-                                          r_out)
-  if (p->dim == 3) {
-    if (p->w == 6) L3ES_GATHER(3, 6);
-    else if (p->w == 8) L3ES_GATHER(3, 8);
-    else L3ES_GATHER(3, 4);
-  } else {
-    if (p->w == 6) L3ES_GATHER(2, 6);
-    else if (p->w == 8) L3ES_GATHER(2, 8);
-    else L3ES_GATHER(2, 4);
-  }
-#undef L3ES_GATHER
-  return cuda_check(cudaGetLastError(), "l3es_interp launch");
+  return cuda_check(cudaGetLastError(), "l3es_interp grid launch");
 }
+
+extern "C" {
 
 int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const double* u_r, int64_t np,
                                   float* u_grid, void* stream) {

@@ -103,12 +103,11 @@ static float2 twiddle(long long m, long long n) {
 // for stage s >= 1 of radix R with Ns points per sub-transform, entries r = 1..R-1,
 // jm = 0..Ns-1 hold exp(-2 pi i r jm / (Ns R)). Same FP64 angles (scaled by powers of
 // two) as the strided table, so both give the same FP32 values.
-static std::vector<float2> twiddles(int n) {
-  std::vector<float2> t(n);
-  for (int m = 0; m < n; ++m) t[m] = twiddle(m, n);
-  const int M = n / 2, E = M >= 8 ? 8 : M;
+// Appends the compact per-stage table of an m-point FFT (radix-8 schedule).
+static void push_compact_table(std::vector<float2>& t, int m) {
+  const int E = m >= 8 ? 8 : m;
   std::vector<int> radix;
-  int rem = M;
+  int rem = m;
   while (E > 1 && rem >= E) {
     radix.push_back(E);
     rem /= E;
@@ -122,6 +121,15 @@ static std::vector<float2> twiddles(int n) {
         for (long long jm = 0; jm < ns; ++jm) t.push_back(twiddle(r * jm, ns * R));
     ns *= R;
   }
+}
+
+// ... followed by the compact table of the n-point FFT (the two-for-one line pass,
+// at line2_ct_offset<n>()).
+static std::vector<float2> twiddles(int n) {
+  std::vector<float2> t(n);
+  for (int m = 0; m < n; ++m) t[m] = twiddle(m, n);
+  push_compact_table(t, n / 2);
+  push_compact_table(t, n);
   return t;
 }
 
@@ -214,6 +222,8 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
     return fail(L3ES_EINVAL, "forcing needs 1 <= kf <= N/4");
   if (desc->kolm_k != 0 && (dim != 2 || desc->kolm_k < 0 || desc->kolm_k >= n / 2))
     return fail(L3ES_EINVAL, "Kolmogorov forcing is 2D with 0 < kolm_k < N/2");
+  if (desc->scheme != L3ES_SCHEME_EXPLICIT && desc->scheme != L3ES_SCHEME_INTEGRATING_FACTOR)
+    return fail(L3ES_EINVAL, "unknown time-stepping scheme " + std::to_string(desc->scheme));
 
   auto* p = new l3es_plan();
   p->desc = *desc;
@@ -417,6 +427,7 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
       prm.kolm_k = d.kolm_k;
       prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
       prm.rk = rk;
+      prm.if_h = d.scheme == L3ES_SCHEME_INTEGRATING_FACTOR ? (float)d.dt : 0.f;
       plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
     }
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
@@ -474,6 +485,7 @@ int l3es_rhs(l3es_plan* plan, const void* u_hat, void* du, void* stream) {
   prm.kolm_k = d.kolm_k;
   prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
   prm.rk = -1;
+  prm.if_h = 0.f;  // rhs_fn itself: the full right-hand side, viscous term included
   plan->tab.stage(plan->ctx, (const float2*)u_hat, nullptr, (float2*)du, -1, prm, (cudaStream_t)stream);
   return cuda_check(cudaGetLastError(), "l3es_rhs launch");
 }

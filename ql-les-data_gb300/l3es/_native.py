@@ -54,6 +54,7 @@ _SIGNATURES = {
     "l3es_interp_coarse_field": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp_coarse_spectrum": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
+    "l3es_interp_advect_rk4": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
     "l3es_interp_particles_to_grid": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
@@ -89,7 +90,12 @@ class PlanDesc(ctypes.Structure):
         ("eps_inj", ctypes.c_double),
         ("drag", ctypes.c_double),
         ("kolm_amp", ctypes.c_double),
+        ("scheme", ctypes.c_int32),
     ]
+
+
+# l3es_plan_desc.scheme: the reference's explicit viscous term, or the integrating factor
+SCHEMES = {"explicit": 0, "integrating_factor": 1}
 
 
 _lib = None
@@ -151,16 +157,18 @@ class Plan:
     def __init__(self, dim: int, n: int, nu: float, dt: float, batch: int = 1,
                  forcing: str = "none", kf: int = 0, e_kin_init: float = 0.0,
                  eps_inj: float = 0.0, drag: float = 0.0, kolm_k: int = 0,
-                 kolm_amp: float = 0.0):
+                 kolm_amp: float = 0.0, scheme: str = "explicit"):
         lib = load()
         if forcing not in FORCING:
             raise ValueError(f"forcing must be one of {list(FORCING)}, got {forcing!r}")
+        if scheme not in SCHEMES:
+            raise ValueError(f"scheme must be one of {list(SCHEMES)}, got {scheme!r}")
         self.dim, self.n, self.batch = int(dim), int(n), int(batch)
         self.nu, self.dt = float(nu), float(dt)
-        self.forcing, self.kf = forcing, int(kf or 0)
+        self.forcing, self.kf, self.scheme = forcing, int(kf or 0), scheme
         d = PlanDesc(self.dim, self.n, self.batch, FORCING[forcing], self.kf, int(kolm_k),
                      self.nu, self.dt, float(e_kin_init), float(eps_inj), float(drag),
-                     float(kolm_amp))
+                     float(kolm_amp), SCHEMES[scheme])
         h = ctypes.c_void_p()
         _check(lib.l3es_plan_create(ctypes.byref(d), ctypes.byref(h)), "l3es_plan_create")
         self._h = h
@@ -370,6 +378,18 @@ class InterpPlan:
             raise ValueError(f"expected (np, {self.dim}) arrays")
         _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend], float(dt),
                                      _ptr(r_out), _stream(stream)), "l3es_interp")
+
+    def advect_rk4(self, r, u_r, dt: float, r_out, backend: str = "nufft", stream=None) -> None:
+        """RK4 particle advection through the current coarse field held fixed over the
+        step (extension; the reference's step is explicit Euler): u_r <- u(r),
+        r_out <- r advanced by one RK4 step of dt."""
+        import torch
+
+        for a in (r, u_r, r_out):
+            if a.dtype != torch.float64 or a.dim() != 2 or a.shape != r.shape or a.shape[-1] != self.dim:
+                raise ValueError(f"positions and velocities are float64 (np, {self.dim})")
+        _check(self._lib.l3es_interp_advect_rk4(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend],
+                                                float(dt), _ptr(r_out), _stream(stream)), "l3es_interp_advect_rk4")
 
     def coarse_mse(self, u_hat_fine, target, loss, grad=None, stream=None) -> None:
         """loss[0] = mean((spectral_filtering(irfftn(u_hat_fine), c) - target)^2) and,

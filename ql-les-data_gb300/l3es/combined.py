@@ -36,8 +36,18 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
              forcing_type="none", e_kin_target=None, kf=None, log_freq=100, vis_freq=100, ckp_freq=100,
              dst_path=None, **ext):
     """Integrate particles along the DNS velocity (combined.py:18-219). Returns the final
-    (u, u_hat, r)."""
+    (u, u_hat, r).
+
+    Extension keyword (besides set_up_solver's): advection='rk4' moves the particles by
+    one classical RK4 step through the step's coarse field held fixed
+    (l3es_interp_advect_rk4) instead of the reference's Euler shift; it cannot be
+    combined with relax_dt_factor > 0, whose relaxation step does its own shift."""
     torch = _torch()
+    advection = ext.pop("advection", "euler")
+    if advection not in ("euler", "rk4"):
+        raise ValueError(f"advection must be 'euler' or 'rk4', got {advection!r}")
+    if advection == "rk4" and (relax_dt_factor or 0.0) > 0.0:
+        raise ValueError("advection='rk4' and SPH relaxation (relax_dt_factor > 0) exclude each other")
     dst_path = dst_path or "results"
     int_path = os.path.join(dst_path, "com")
     os.makedirs(int_path, exist_ok=True)
@@ -86,7 +96,9 @@ def combined(case, N=256, dim=3, nu=0.000625, t_final=0.1, t_burnin=0, dt=0.01, 
         # u_lres = spectral_filtering(u_hres, ckp_N); u_r = interpolator(u_lres, r);
         # r_next = shift_fn(r, dt * u_r)   (combined.py:122-130, :199)
         ip.set_spectrum(u_hat)
-        if relax is None:
+        if advection == "rk4":
+            ip.advect_rk4(r, u_r, dt, r_next, backend=interp_backend)
+        elif relax is None:
             ip.interp(r, u_r, backend=interp_backend, dt=dt, r_out=r_next)
         else:
             # u_r_0 kept for the checkpoint; particles advance with the relaxed velocity

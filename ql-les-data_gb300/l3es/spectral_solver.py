@@ -194,7 +194,9 @@ def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None, forc
 
     Extension keywords (no reference counterpart): spectrum='k4exp', kp (HIT init),
     drag, kolm_k, kolm_amp (2D Kolmogorov forcing), eps_inj (constant-power forcing on
-    0 < |k| <= kf, selected with forcing_type='const_power')."""
+    0 < |k| <= kf, selected with forcing_type='const_power'), scheme='integrating_factor'
+    (the viscous term integrated exactly by exp(-nu k^2 t) instead of the reference's
+    explicit term; default 'explicit')."""
     torch = _torch()
     L = 2 * np.pi
     dx = L / N
@@ -205,7 +207,7 @@ def set_up_solver(N, nu, dim, case, dt, seed, ckp_N, kf, e_kin_target=None, forc
     if dim == 2:
         xyz_vis = (xyz_vis.T + np.array([0, 0, L - dx])).T
     init_ext = {k: ext[k] for k in ("spectrum", "kp", "init", "init_kmax", "init_energy", "kolm_grid") if k in ext}
-    plan_ext = {k: ext[k] for k in ("drag", "kolm_k", "kolm_amp", "eps_inj") if k in ext}
+    plan_ext = {k: ext[k] for k in ("drag", "kolm_k", "kolm_amp", "eps_inj", "scheme") if k in ext}
     u = _initial_field(case, N, dim, seed, init_ext)
     e_kin_init = 0.5 * np.mean(np.sum(u * u, axis=0))
     if forcing_type != "none":

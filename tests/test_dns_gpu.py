@@ -317,3 +317,101 @@ def test_nonfinite_state_is_reported_and_cleared(dim, n):
     p.step(uh, 2)
     assert lib.l3es_plan_check(p._h) == 0
     assert torch.isfinite(torch.view_as_real(uh)).all()
+
+
+def _band_limited(dim, n, seed, kmax=6):
+    rng = np.random.default_rng(seed)
+    shape = (3, n, n, n) if dim == 3 else (3, n, n, 1)
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    u = rng.standard_normal(shape)
+    if dim == 2:
+        u[2] = 0.0
+    uh = np.fft.rfftn(u, axes=axes)
+    k = np.fft.fftfreq(n, 1.0 / n)
+    kh = np.arange(n // 2 + 1)
+    if dim == 3:
+        kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kh[None, None, :] ** 2)
+    else:
+        kk = np.sqrt(k[:, None, None] ** 2 + kh[None, :, None] ** 2)
+    uh = np.where(kk <= kmax, uh, 0.0)
+    u = np.fft.irfftn(uh, s=(n,) * dim, axes=axes)
+    if dim == 2:
+        u = u.reshape(3, n, n, 1)
+    return u / np.abs(u).max()
+
+
+@pytest.mark.parametrize("dim,n", [(3, 32), (2, 64)])
+def test_integrating_factor_step_matches_oracle(dim, n):
+    """Extension: RK4 with the viscous term by the integrating factor exp(-nu k^2 t)
+    vs the oracle's Lawson RK4 (rk4_if_wrapper), a few steps (2D with drag and
+    Kolmogorov forcing)."""
+    nu, dt, steps = 0.02, 5e-3, 3
+    u = _band_limited(dim, n, 11)
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    uh0 = np.fft.rfftn(u, axes=axes)
+    kw, okw = {}, {}
+    if dim == 2:
+        uh0 = uh0.squeeze(-1)
+        kw = dict(drag=0.1, kolm_k=4, kolm_amp=1.0)
+        okw = dict(drag=0.1, force_hat=R.kolmogorov_forcing_hat(n, 1.0, 4))
+    step = R.rk4_if_wrapper(dt, R.rhs_wrapper(n, 0.0, axes, **okw), nu, n, axes)
+    uu, uh = u, uh0
+    for _ in range(steps):
+        uu, uh, _ = step(uu, uh)
+    p = _plan(dim=dim, n=n, nu=nu, dt=dt, scheme="integrating_factor", **kw)
+    g = _c64(uh0)
+    p.step(g, steps)
+    p.check()
+    assert _rel(g.cpu().numpy(), uh) < RTOL
+    # and it differs from the explicit form by the (small) truncation difference only
+    q = _plan(dim=dim, n=n, nu=nu, dt=dt, **kw)
+    ge = _c64(uh0)
+    q.step(ge, steps)
+    assert _rel(ge.cpu().numpy(), uh) < 1e-3
+
+
+def test_integrating_factor_is_stable_where_explicit_rk4_blows_up():
+    """nu k^2 dt far above explicit RK4's stability limit (~2.8) for the high modes:
+    the explicit step produces non-finite values (reported as NonFiniteError), the
+    integrating-factor step stays finite and matches the oracle."""
+    from l3es import _native
+
+    n, nu, dt, steps = 32, 0.2, 0.05, 40  # nu k^2 dt up to 0.2 * 0.05 * 768 = 7.7 on the grid
+    u = _band_limited(3, n, 12, kmax=4)
+    uh0 = np.fft.rfftn(u, axes=(1, 2, 3))
+    pe = _plan(dim=3, n=n, nu=nu, dt=dt)
+    rng = np.random.default_rng(0)
+    noise = 1e-6 * (rng.standard_normal(uh0.shape) + 1j * rng.standard_normal(uh0.shape))
+    ge = _c64(uh0 + noise)  # round-off-sized content in the stiff modes
+    for _ in range(20):
+        pe.step(ge, steps)
+        try:
+            pe.check()
+        except _native.NonFiniteError:
+            break
+    else:
+        pytest.fail("the explicit step stayed finite where it should be unstable")
+    step = R.rk4_if_wrapper(dt, R.rhs_wrapper(n, 0.0), nu, n)
+    uu, uh = u, uh0 + noise
+    for _ in range(steps):
+        uu, uh, _ = step(uu, uh)
+    pi = _plan(dim=3, n=n, nu=nu, dt=dt, scheme="integrating_factor")
+    gi = _c64(uh0 + noise)
+    pi.step(gi, steps)
+    pi.check()
+    assert _rel(gi.cpu().numpy(), uh) < 1e-4
+
+
+def test_integrating_factor_decays_a_shear_mode_exactly():
+    """u = (sin y, 0, 0): the nonlinear term is a pure gradient, so the exact solution
+    is exp(-nu t) u; the integrating-factor step reproduces it to FP32 rounding."""
+    n, nu, dt, steps = 32, 0.5, 0.1, 10
+    y = np.arange(n) * 2 * np.pi / n
+    u = np.zeros((3, n, n, n))
+    u[0] = np.sin(y)[None, :, None]
+    p = _plan(dim=3, n=n, nu=nu, dt=dt, scheme="integrating_factor")
+    g = _c64(np.fft.rfftn(u, axes=(1, 2, 3)))
+    p.step(g, steps)
+    out = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
+    p.irfftn(g, out)
+    assert np.abs(out.cpu().numpy() - np.exp(-nu * dt * steps) * u).max() < 1e-6

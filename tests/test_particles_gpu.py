@@ -121,3 +121,51 @@ def test_shift_matches_reference_golden(gold):
     g = gold("interp")
     out = _native.shift(_t(g["r3"], np.float64), _t(g["dr"], np.float64))
     assert np.abs(out.cpu().numpy() - g["shifted"]).max() < 1e-14
+
+
+def _band_field(dim, c, seed):
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((3,) + (c,) * dim)
+    axes = tuple(range(1, dim + 1))
+    gh = np.fft.fftn(g, axes=axes)
+    k = np.fft.fftfreq(c, 1.0 / c)
+    kk = np.sqrt(sum(np.meshgrid(*([k ** 2] * dim), indexing="ij")))
+    g = np.real(np.fft.ifftn(gh * (kk <= c / 4), axes=axes))
+    return g / np.abs(g).max()
+
+
+@pytest.mark.parametrize("dim,c,np_", [(3, 16, 700), (2, 32, 1024)])
+def test_rk4_advection_matches_oracle(dim, c, np_):
+    """Extension: RK4 particle advection through the coarse field held fixed, both
+    backends, vs the oracle's advect_rk4 over the exact DFT interpolant."""
+    g = _band_field(dim, c, 40 + dim)
+    comp = g[:dim] if dim == 2 else g
+    rng = np.random.default_rng(5)
+    r = rng.uniform(0, 2 * np.pi, (np_, dim))
+    dt = 0.2
+    u_ref, r_ref = R.advect_rk4(lambda x: R.interpolate_dft(comp, x), r, dt)
+    p = _plan(dim=dim, ckp_n=c, np_max=np_)
+    p.set_field(_t(g if dim == 3 else g[..., None], np.float32))
+    rt = _t(r, np.float64)
+    for backend, tol in (("dft", 2e-5), ("nufft", 5e-5)):
+        ur = torch.empty_like(rt)
+        rn = torch.empty_like(rt)
+        p.advect_rk4(rt, ur, dt, rn, backend=backend)
+        assert _rel(ur.cpu().numpy(), u_ref) < tol, backend
+        d = np.mod(rn.cpu().numpy() - r_ref + np.pi, 2 * np.pi) - np.pi
+        assert np.abs(d).max() < tol * dt * np.abs(u_ref).max(), backend
+        assert (rn.cpu().numpy() >= 0).all() and (rn.cpu().numpy() < 2 * np.pi).all()
+    # the Euler step of l3es_interp differs from RK4 at second order in dt
+    ur = torch.empty_like(rt)
+    re = torch.empty_like(rt)
+    p.interp(rt, ur, backend="dft", dt=dt, r_out=re)
+    de = np.mod(re.cpu().numpy() - r_ref + np.pi, 2 * np.pi) - np.pi
+    assert np.abs(de).max() > 100 * 2e-5 * dt * np.abs(u_ref).max()
+
+
+def test_rk4_advection_rejects_aliased_outputs():
+    p = _plan(dim=3, ckp_n=16, np_max=64)
+    r = torch.zeros(64, 3, dtype=torch.float64, device="cuda")
+    u = torch.empty_like(r)
+    with pytest.raises(RuntimeError, match="separate"):
+        p.advect_rk4(r, u, 0.1, r)
