@@ -205,6 +205,18 @@ int l3es_interp(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r
 int l3es_interp_advect_rk4(l3es_interp_plan* plan, const double* r, int64_t np, double* u_r,
                            int32_t backend, double dt, double* r_out, void* stream);
 
+/* Reverse mode of the particle interpolation: the reference differentiates
+ * interpolate_finufft / interpolate_dft (integrator.py:36-91) after
+ * spectral_filtering (utils.py:100-138) with jax.grad; here, for the velocities u_r of
+ * l3es_interp_set_spectrum + l3es_interp at fixed positions r, and a cotangent
+ * lam = dL/du_r (float64, (np, dim)), grad_fine receives dL/du_hat_fine (complex64,
+ * the fine spectrum's shape, overwritten; convention of the adjoint calls below).
+ * backend 0: the adjoint of the NUFFT (type-1 spread with the ES kernel, forward FFT of
+ * the upsampled grid, deconvolution); 1: of the exact DFT. The plan needs n_fine > 0;
+ * its coarse spectrum is not changed. */
+int l3es_interp_vjp(l3es_interp_plan* plan, const double* r, int64_t np, const double* lam,
+                    int32_t backend, void* grad_fine, void* stream);
+
 /* Allocation-free form of l3es_interp_set_spectrum + l3es_interp(backend dft): no
  * counterpart in the reference. For hosts that cannot let a library allocate
  * device memory (e.g. a JAX/XLA FFI custom call, whose device memory belongs to
@@ -240,10 +252,12 @@ int l3es_shift(const double* r, const double* dr, int64_t n, double scale, doubl
  * (l3es/spectral_solver.py:50-80); here they are hand-written vector-Jacobian
  * products. Gradients of a real loss L with respect to a complex64 half spectrum z
  * use the convention dL/dRe z + i dL/dIm z (PyTorch's), i.e.
- * dL = Re sum(conj(grad) dz) over the stored entries. Supported forcings: none and
- * const_power (with drag and the Kolmogorov term); ekin_tot returns L3ES_EINVAL.
- * The first call allocates the plan's adjoint workspace (10 spectra of the plan's
- * size); l3es_plan_adjoint_prepare does it ahead of time (before any capture). */
+ * dL = Re sum(conj(grad) dz) over the stored entries. Supported forcings: none,
+ * const_power (with drag and the Kolmogorov term) and ekin_tot (the kinetic-energy
+ * rescaling after each step, spectral_solver.py:82-112, is differentiated: its adjoint
+ * recomputes the step's last stage); plans with L3ES_SCHEME_INTEGRATING_FACTOR return
+ * L3ES_EINVAL. The first call allocates the plan's adjoint workspace (10 spectra of the
+ * plan's size); l3es_plan_adjoint_prepare does it ahead of time (before any capture). */
 int l3es_plan_adjoint_prepare(l3es_plan* plan);
 
 /* out = (d rhs / d u_hat)^T g at u_hat (the adjoint of l3es_rhs). */

@@ -104,6 +104,39 @@ def rk4_step_vjp(u_hat0, lam1, dt, rhs_fn, vjp_fn):
     return lam
 
 
+def ekin_tot_forward(u_rk, mask, e0, N, dim):
+    """The ekin_tot rescaling after the RK4 update (spectral_solver.py:82-112) in the
+    Parseval form: E = sum w |u_hat|^2 / (2 N^(2d)) over the stored modes, E_low over the
+    band (mask), alpha = sqrt(max(0, (E0 - (E - E_low)) / (E_low + eps)));
+    u_new = u_rk (alpha mask + 1 - mask). Returns (u_new, alpha, E_high, E_low)."""
+    w = _w(N, dim)
+    nd = float(N) ** (2 * dim)
+    e_all = np.sum(w * np.sum(np.abs(u_rk) ** 2, axis=0)) / (2.0 * nd)
+    e_low = np.sum(w * np.sum(np.abs(u_rk * mask) ** 2, axis=0)) / (2.0 * nd)
+    e_high = e_all - e_low
+    alpha = np.sqrt(max(0.0, (e0 - e_high) / (e_low + R.EPS)))
+    return u_rk * (alpha * mask + (1 - mask)), alpha, e_high, e_low
+
+
+def ekin_tot_vjp(u_rk, lam, mask, e0, N, dim):
+    """Adjoint of ekin_tot_forward at u_rk for the cotangent lam of u_new:
+    with beta = Re sum_band conj(lam) u_rk and d alpha = (1 / (2 alpha)) (-dE_high / (E_low + eps)
+    - (E0 - E_high) dE_low / (E_low + eps)^2), dE = Re sum w conj(u_rk) du / N^(2d):
+        lam_rk = (1 - mask) (lam - c_h w u_rk) + mask (alpha lam - c_l w u_rk),
+        c_h = beta / (2 alpha (E_low + eps) N^(2d)),  c_l = beta alpha / (2 (E_low + eps) N^(2d))
+    (alpha = 0, where the rescaling saturates, contributes no alpha term)."""
+    w = _w(N, dim)
+    nd = float(N) ** (2 * dim)
+    _, alpha, e_high, e_low = ekin_tot_forward(u_rk, mask, e0, N, dim)
+    beta = float(np.real(np.sum(np.conj(lam) * u_rk * mask)))
+    if alpha > 0.0:
+        c_h = beta / (2.0 * alpha * (e_low + R.EPS) * nd)
+        c_l = beta * alpha / (2.0 * (e_low + R.EPS) * nd)
+    else:
+        c_h = c_l = 0.0
+    return (1 - mask) * (lam - c_h * w * u_rk) + mask * (alpha * lam - c_l * w * u_rk)
+
+
 def coarse_mse(u_hat, target, c, fft_axes=(1, 2, 3)):
     """mean((spectral_filtering(irfftn(u_hat), c) - target)^2) over the dim velocity
     components (utils.py:100-138 for the coarsening)."""
@@ -131,15 +164,13 @@ def _box_count(N, c, dim):
     return a.astype(np.float64) + b.astype(np.float64)
 
 
-def coarse_mse_grad(u_hat, target, c, fft_axes=(1, 2, 3)):
-    """Gradient of coarse_mse with respect to the fine half spectrum u_hat:
-    G = (w / (2 N^d)) n(k) V(k), V = rfftn_c(2 (u_c - target) / size) read at
-    (kx mod c, ky mod c, kz); components beyond dim are zero."""
+def coarse_field_vjp(v, N, c, fft_axes=(1, 2, 3), ncomp=3):
+    """Adjoint of u_hat -> spectral_filtering(irfftn(u_hat), c) (utils.py:100-138): the
+    gradient with respect to the fine half spectrum of L = sum(v * u_c) for a real
+    coarse-grid cotangent v (dim, c, ...):
+    G = (w / (2 N^d)) n(k) V(k), V = rfftn_c(v) read at (kx mod c, ky mod c, kz);
+    components beyond dim are zero."""
     dim = len(fft_axes)
-    N = u_hat.shape[1]
-    u = R._irfftn(u_hat, axes=fft_axes)[:dim]
-    uc = R.spectral_filtering(u, c)
-    v = 2.0 * (uc - target) / uc.size
     V = np.fft.rfftn(v, axes=fft_axes)
     H = N // 2 + 1
     ix = np.arange(N) % c
@@ -149,9 +180,41 @@ def coarse_mse_grad(u_hat, target, c, fft_axes=(1, 2, 3)):
     else:
         Vf = V[:, ix][:, :, kz]
     n = _box_count(N, c, dim)
-    G = np.zeros(u_hat.shape, dtype=np.complex128)
+    shape = (ncomp, N, N, H) if dim == 3 else (ncomp, N, H)
+    G = np.zeros(shape, dtype=np.complex128)
     G[:dim] = (_w(N, dim) / (2.0 * float(N) ** dim)) * n * Vf
     return G
+
+
+def coarse_mse_grad(u_hat, target, c, fft_axes=(1, 2, 3)):
+    """Gradient of coarse_mse with respect to the fine half spectrum u_hat (the
+    coarse-field adjoint of the residual 2 (u_c - target) / size)."""
+    dim = len(fft_axes)
+    N = u_hat.shape[1]
+    u = R._irfftn(u_hat, axes=fft_axes)[:dim]
+    uc = R.spectral_filtering(u, c)
+    v = 2.0 * (uc - target) / uc.size
+    return coarse_field_vjp(v, N, c, fft_axes, ncomp=u_hat.shape[0])
+
+
+def interp_vjp(lam, r, N, c, fft_axes=(1, 2, 3)):
+    """Gradient with respect to the fine half spectrum of L = sum(lam * u_r), u_r the
+    particle velocities of the combined loop (spectral_filtering to c, then the exact
+    spectral interpolation of integrator.py:62-91 at r; interpolate_from_uhat_dft).
+    lam, r: (Np, dim). The interpolation u_r = Re sum_k U(k) exp(i k.r) / c^d over the
+    c^d modes of U = fftn(u_c) has the coarse-grid adjoint
+        v(x) = Re sum_k Ubar(k) exp(i k.x),  Ubar(k) = sum_j lam_j exp(-i k.r_j) / c^d,
+    which then goes through coarse_field_vjp."""
+    dim = len(fft_axes)
+    k = np.fft.fftfreq(c, 1.0 / c)
+    ph = [np.exp(-1j * r[:, d, None] * k[None, :]) for d in range(dim)]  # (Np, c) per axis
+    if dim == 3:
+        ub = np.einsum("jc,ja,jb,jz->cabz", lam, ph[0], ph[1], ph[2])
+    else:
+        ub = np.einsum("jc,ja,jb->cab", lam, ph[0], ph[1])
+    ub /= float(c) ** dim
+    v = np.real(np.fft.ifftn(ub, axes=fft_axes)) * float(c) ** dim
+    return coarse_field_vjp(v, N, c, fft_axes)
 
 
 def trajectory_loss_and_grad(u_hat0, nsteps, dt, rhs_fn, vjp_fn, target, c, fft_axes=(1, 2, 3)):

@@ -556,6 +556,23 @@ struct Line2Cfg {
   static constexpr int XS = xpad_len<1>(N);   // exchange slots per line slot
 };
 
+// L1 prefetch of the six field lines of one line (H float2 each, fs apart): 9 prefetches
+// of 128 bytes cover a 1032-byte line at any 8-byte offset; lanes share the 54.
+template <int N>
+__device__ __forceinline__ void prefetch_line6(const float2* src, long long fs, int t) {
+  constexpr int T = N / 8, H = N / 2 + 1, CH = (H * 8 + 127) / 128 + ((H * 8) % 128 ? 1 : 0);
+  for (int k = t; k < 6 * CH; k += T) {
+    const int f = k / CH, q = k % CH;
+    const float2* a = src + f * fs + (q * 16 < H ? q * 16 : H - 1);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+  }
+}
+
+// Persistent: each line slot (T lanes) walks line pairs (A, B) slot + k * slots_total,
+// counted from the last line, and prefetches into L1 the six input lines of the next line
+// it will transform (B while A runs, the next pair's A while B runs), so the loads of a
+// pair hit L1 instead of waiting on L2 / DRAM (the kernel's registers leave no room for a
+// register prefetch).
 template <int N>
 __global__ void __launch_bounds__(Line2Cfg<N>::THREADS, 4)
 line_cross2(const float2* __restrict__ w, long long fs, float2* __restrict__ du, long long ds, int kt, int kd,
@@ -568,58 +585,69 @@ line_cross2(const float2* __restrict__ w, long long fs, float2* __restrict__ du,
   float2* xs = s_x + slot * C::XS;
   const float2* wb = w + (long long)blockIdx.y * 6 * fs;
   float2* db = du + (long long)blockIdx.y * 3 * ds;
-  const long long ia = 2 * ((long long)blockIdx.x * C::SLOTS + slot);  // line A; B = A + 1
-  float pa[8], pb[8];  // z component of u x curl u of lines A and B
+  const long long npairs = (nlines + 1) / 2;
+  const long long stride = (long long)gridDim.x * C::SLOTS;
+  long long pair = (long long)blockIdx.x * C::SLOTS + slot;
+  if (pair < npairs) prefetch_line6<N>(wb + (long long)(nlines - 1 - 2 * pair) * H, fs, t);
+#pragma unroll 1
+  for (; pair < npairs; pair += stride) {
+    const long long ia = 2 * pair;  // line A (counted from the last line); B = A + 1
+    float pa[8], pb[8];              // z component of u x curl u of lines A and B
 #pragma unroll
-  for (int half = 0; half < 2; ++half) {
-    const long long idx = ia + half;
-    const bool valid = idx < nlines;
-    const long long line = valid ? nlines - 1 - idx : nlines - 1;  // idle slots mirror a valid line
-    const float2* src = wb + line * H;
-    float2 h1[8], h2[8], z[8];
-    c2r_pair_load<N>(src, src + fs, t, z);  // u_x + i u_y
-    warp_fft<N, 8, kInv>(z, xs, t, ct);
+    for (int half = 0; half < 2; ++half) {
+      const long long idx = ia + half;
+      const bool valid = idx < nlines;
+      const long long line = valid ? nlines - 1 - idx : nlines - 1;  // an odd last pair mirrors a valid line
+      // prefetch the line transformed after this one: B, or the next pair's A
+      const long long nxt = half == 0 ? ia + 1 : ia + 2 * stride;
+      if (nxt < nlines) prefetch_line6<N>(wb + (nlines - 1 - nxt) * H, fs, t);
+      const float2* src = wb + line * H;
+      float2 h1[8], h2[8], z[8];
+      c2r_pair_load<N>(src, src + fs, t, z);  // u_x + i u_y
+      warp_fft<N, 8, kInv>(z, xs, t, ct);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) h1[e] = z[e];
-    __syncwarp();
-    c2r_pair_load<N>(src + 2 * fs, src + 3 * fs, t, z);  // u_z + i curl_x
-    warp_fft<N, 8, kInv>(z, xs, t, ct);
+      for (int e = 0; e < 8; ++e) h1[e] = z[e];
+      __syncwarp();
+      c2r_pair_load<N>(src + 2 * fs, src + 3 * fs, t, z);  // u_z + i curl_x
+      warp_fft<N, 8, kInv>(z, xs, t, ct);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) h2[e] = z[e];
-    __syncwarp();
-    c2r_pair_load<N>(src + 4 * fs, src + 5 * fs, t, z);  // curl_y + i curl_z
-    warp_fft<N, 8, kInv>(z, xs, t, ct);
-    __syncwarp();
-    // u x curl u at this lane's positions (unnormalised: the scale enters in s2)
+      for (int e = 0; e < 8; ++e) h2[e] = z[e];
+      __syncwarp();
+      c2r_pair_load<N>(src + 4 * fs, src + 5 * fs, t, z);  // curl_y + i curl_z
+      warp_fft<N, 8, kInv>(z, xs, t, ct);
+      __syncwarp();
+      // u x curl u at this lane's positions (unnormalised: the scale enters in s2)
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const float ux = h1[e].x, uy = h1[e].y, uz = h2[e].x, wx = h2[e].y, wy = z[e].x, wz = z[e].y;
-      const float pz = fmaf(ux, wy, -uy * wx);
-      if (half == 0)
-        pa[e] = pz;
-      else
-        pb[e] = pz;
-      z[e] = make_float2(fmaf(uy, wz, -uz * wy), fmaf(uz, wx, -ux * wz));
+      for (int e = 0; e < 8; ++e) {
+        const float ux = h1[e].x, uy = h1[e].y, uz = h2[e].x, wx = h2[e].y, wy = z[e].x, wz = z[e].y;
+        const float pz = fmaf(ux, wy, -uy * wx);
+        if (half == 0)
+          pa[e] = pz;
+        else
+          pb[e] = pz;
+        z[e] = make_float2(fmaf(uy, wz, -uz * wy), fmaf(uz, wx, -ux * wz));
+      }
+      warp_fft<N, 8, kFwd>(z, xs, t, ct);
+      float2 X[4], Y[4];
+      r2c_pair_unpack<N>(z, t, s2, X, Y);
+      if (valid) {
+        float2* dst = db + line * kt;
+        store_du_line<N>(dst, X, t, kt, kd);
+        store_du_line<N>(dst + ds, Y, t, kt, kd);
+      }
+      __syncwarp();
     }
+    // z components of lines A and B in one forward FFT
+    float2 z[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) z[e] = make_float2(pa[e], pb[e]);
     warp_fft<N, 8, kFwd>(z, xs, t, ct);
     float2 X[4], Y[4];
     r2c_pair_unpack<N>(z, t, s2, X, Y);
-    if (valid) {
-      float2* dst = db + line * kt;
-      store_du_line<N>(dst, X, t, kt, kd);
-      store_du_line<N>(dst + ds, Y, t, kt, kd);
-    }
+    store_du_line<N>(db + 2 * ds + (nlines - 1 - ia) * kt, X, t, kt, kd);
+    if (ia + 1 < nlines) store_du_line<N>(db + 2 * ds + (nlines - 2 - ia) * kt, Y, t, kt, kd);
     __syncwarp();
   }
-  // z components of lines A and B in one forward FFT
-  float2 z[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) z[e] = make_float2(pa[e], pb[e]);
-  warp_fft<N, 8, kFwd>(z, xs, t, ct);
-  float2 X[4], Y[4];
-  r2c_pair_unpack<N>(z, t, s2, X, Y);
-  if (ia < nlines) store_du_line<N>(db + 2 * ds + (nlines - 1 - ia) * kt, X, t, kt, kd);
-  if (ia + 1 < nlines) store_du_line<N>(db + 2 * ds + (nlines - 2 - ia) * kt, Y, t, kt, kd);
 }
 
 // ------------------------------------------------------------------------------
@@ -994,8 +1022,10 @@ kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2
 //   rk 3   : fin <- acc + a dt du
 //   rk -1  : out <- du (the reference's rhs_fn)
 // Every thread loads all its operands before storing (us/out and acc alias).
+// VIF: the integrating-factor form (a separate instantiation, so the reference's explicit
+// form keeps its own code).
 // ------------------------------------------------------------------------------
-template <int N, int DIM>
+template <int N, int DIM, bool VIF = false>
 __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a0, float2 z0,
                                           const float2* __restrict__ P, long long pcs, int kt, int kd,
                                           const EpiParams& prm, float fscale, float2& nv) {
@@ -1020,7 +1050,7 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
     const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
     r = __ldg(P + c * pcs + row * kt + kh);
   }
-  const bool vif = prm.if_h > 0.f && prm.rk >= 0;
+  const bool vif = VIF && prm.rk >= 0;
   if (!vif) {
     r.x -= nu * kk2 * sv.x;
     r.y -= nu * kk2 * sv.y;
@@ -1086,7 +1116,7 @@ __device__ __forceinline__ float2 rk_elem(unsigned i, int c, float2 sv, float2 a
 // The last stage (rk 3) also flags a non-finite value of the new state in *err
 // (kErrNonFinite): the blow-up check of the drivers, one add and one compare per
 // thread, no extra pass.
-template <int N, int DIM>
+template <int N, int DIM, bool VIF = false>
 __global__ void __launch_bounds__(256)
 k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const float2* us, const float2* u0,
             float2* acc, float2* out, float2* fin, long long cs, EpiParams prm,
@@ -1107,9 +1137,9 @@ k_rk_update(const float2* __restrict__ P, long long pcs, int kt, int kd, const f
     float2 nv0, nv1;
     const unsigned ucs = (unsigned)cs, ug = (unsigned)g;
     const int c0 = (int)(ug / ucs), c1 = (int)((ug + 1u) / ucs);
-    const float2 r0 = rk_elem<N, DIM>(ug - (unsigned)c0 * ucs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
+    const float2 r0 = rk_elem<N, DIM, VIF>(ug - (unsigned)c0 * ucs, c0, make_float2(s4.x, s4.y), make_float2(a4.x, a4.y),
                                       make_float2(z4.x, z4.y), Pb, pcs, kt, kd, prm, fscale, nv0);
-    const float2 r1 = rk_elem<N, DIM>(ug + 1u - (unsigned)c1 * ucs, c1, make_float2(s4.z, s4.w),
+    const float2 r1 = rk_elem<N, DIM, VIF>(ug + 1u - (unsigned)c1 * ucs, c1, make_float2(s4.z, s4.w),
                                       make_float2(a4.z, a4.w), make_float2(z4.z, z4.w), Pb, pcs, kt, kd, prm,
                                       fscale, nv1);
     if (prm.rk < 0) {

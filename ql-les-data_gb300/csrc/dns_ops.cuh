@@ -37,11 +37,24 @@ struct DnsOps {
     return 0;
   }
 
+  // resident CTAs (all SMs) of the persistent two-for-one line pass (0: one CTA per tile)
+  static inline int line2_ctas = 0;
+
   static void init_attrs() {
     if constexpr (N >= 64) {
       tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
       tma_plain_ctas = persistent_ctas(kx_inv_tma<N, false>);
+    }
+    if constexpr (N >= 64 && N <= 256) {
+      int nb = 0, dev = 0, sms = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, line_cross2<N>, Line2Cfg<N>::THREADS, 0) ==
+              cudaSuccess &&
+          cudaGetDevice(&dev) == cudaSuccess &&
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+        line2_ctas = nb * sms;
+      else
+        cudaGetLastError();
     }
   }
 
@@ -84,11 +97,13 @@ struct DnsOps {
     if (DIM == 3)
       L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
                   ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
-    if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT
+    if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT, persistent
       using L2 = Line2Cfg<N>;
       const float s2 = 0.5f * scale * scale;
+      const long long tiles = (lines + L2::LPC - 1) / L2::LPC;
+      const long long cap = line2_ctas > 0 ? std::max(1, line2_ctas / c.batch) : tiles;
       L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
-                  line_cross2<N><<<dim3((unsigned)((lines + L2::LPC - 1) / L2::LPC), c.batch), L2::THREADS, 0, s>>>(
+                  line_cross2<N><<<dim3((unsigned)std::min(tiles, cap), c.batch), L2::THREADS, 0, s>>>(
                       c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines));
     } else {
       L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
@@ -131,9 +146,15 @@ struct DnsOps {
     // 3: us, acc -> fin
     const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);
     const long long pairs = 3 * c.cs / 2;
-    L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
-                k_rk_update<N, DIM><<<dim3((unsigned)((pairs + 255) / 256), c.batch), 256, 0, s>>>(
-                    c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm, c.band, c.nu_b, c.err));
+    const dim3 ug((unsigned)((pairs + 255) / 256), c.batch);
+    if (prm.if_h > 0.f && rk >= 0)
+      L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
+                  k_rk_update<N, DIM, true><<<ug, 256, 0, s>>>(c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm,
+                                                                c.band, c.nu_b, c.err));
+    else
+      L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
+                  k_rk_update<N, DIM><<<ug, 256, 0, s>>>(c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm,
+                                                          c.band, c.nu_b, c.err));
   }
 
   static void stage(const Ctx& c, const float2* us, float2* S, float2* out, int rk, const EpiParams& prm,

@@ -173,6 +173,7 @@ struct AdjWork {
   float2* LAM = nullptr;  // [batch][3][cs] accumulated cotangent
   float2* G = nullptr;    // [batch][3][cs] stage cotangent
   double* band = nullptr; // [batch][2]
+  double* ekin = nullptr; // [batch][3] ekin_tot adjoint: alpha, c_high, c_low
   std::vector<void*> allocs;
 };
 
@@ -196,6 +197,10 @@ template <int N>
 DnsTable make_dns_table();
 bool dns_table(int n, DnsTable* out);  // false if N is not compiled in
 const Ctx& plan_ctx(const l3es_plan* p);
+
+// Per-block float-float partial sums of w |u_hat|^2 of the plan's trajectories into
+// c.partial ([batch][nblk]); returns nblk (plan.cu).
+int energy_partials(const Ctx& c, const float2* uh, cudaStream_t s);
 
 // thread-local error reporting
 void set_error(const std::string& msg);

@@ -248,6 +248,166 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
 }
 
 // ------------------------------------------------------------------------------
+// Adjoint of the particle interpolation (u_r of l3es_interp as a function of the fine
+// half spectrum, at fixed positions), for a cotangent lam = dL/du_r (np, dim):
+//   NUFFT: spread (the transpose of k_nufft_gather) -> forward FFT of the n-grid ->
+//          k_box_to_half_adj with the deconvolution factors -> k_crop_adj
+//   DFT:   k_p2g_dft (sum_j lam_j exp(-i k.r_j) on the c-grid) -> k_box_to_half_adj
+//          -> k_crop_adj
+// Gradients of complex arrays follow dL = Re sum conj(grad) d(array).
+// ------------------------------------------------------------------------------
+// gbar[comp](l) += norm lam[j][comp] prod_d phi((x_d / h - l_d) / (w / 2)); lanes as
+// in the gather (lane q < W: support column q of the contiguous axis, all outer rows).
+// FP32 atomic additions: the order of a grid point's contributions is not fixed.
+template <int DIM, int W>
+__global__ void __launch_bounds__(128)
+k_nufft_spread(float* __restrict__ gbar, long long gcs, int n, int ncomp, float beta, double norm,
+               const double* __restrict__ r, const int* __restrict__ perm, long long np,
+               const double* __restrict__ lam) {
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = gt / kGatherLanes;
+  const int a = (int)(gt % kGatherLanes);
+  if (i >= np || a >= W) return;
+  const long long j = perm ? perm[i] : i;
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  const double inv_h = n / two_pi;
+  float wk[DIM][W];
+  int id[DIM][W];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const double xs = r[j * DIM + d] * inv_h;
+    const double l0 = ceil(xs - 0.5 * W);
+    const int il0 = (int)l0;
+    const float t = (float)(xs - l0);
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+      const float z = (t - (float)q) * (2.0f / W);
+      const float qq = 1.f - z * z;
+      wk[d][q] = qq > 0.f ? expf(beta * (sqrtf(qq) - 1.f)) : 0.f;
+      id[d][q] = (il0 + q) & (n - 1);
+    }
+  }
+  float wl = 0.f;
+  int il = 0;
+#pragma unroll
+  for (int q = 0; q < W; ++q)
+    if (q == a) {
+      wl = wk[DIM - 1][q];
+      il = id[DIM - 1][q];
+    }
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const float v = (float)(norm * lam[j * ncomp + comp]) * wl;
+    float* gc = gbar + comp * gcs + il;
+    if (DIM == 3) {
+#pragma unroll
+      for (int q0 = 0; q0 < W; ++q0) {
+        const float v0 = v * wk[0][q0];
+#pragma unroll
+        for (int q1 = 0; q1 < W; ++q1) atomicAdd(gc + ((long long)id[0][q0] * n + id[1][q1]) * n, v0 * wk[1][q1]);
+      }
+    } else {
+#pragma unroll
+      for (int q0 = 0; q0 < W; ++q0) atomicAdd(gc + (long long)id[0][q0] * n, v * wk[0][q0]);
+    }
+  }
+}
+
+// forward c2c FFT of contiguous lines of NL real values (imaginary part zero)
+template <int NL>
+__global__ void __launch_bounds__(128)
+line_fft_real_fwd(const float* __restrict__ x, float2* __restrict__ g, long long nlines,
+                  const float2* __restrict__ tw) {
+  constexpr int E = Fft<NL>::E, T = Fft<NL>::T;
+  static_assert(T <= 32, "line inside one warp");
+  constexpr int LPC = (32 / T) * 4;
+  constexpr int XS = xpad_len<1>(NL);
+  __shared__ float2 s_x[LPC * XS];
+  const int q = threadIdx.x / T, t = threadIdx.x % T;
+  const long long line_raw = (long long)blockIdx.x * LPC + q;
+  const bool valid = line_raw < nlines;
+  const long long line = valid ? line_raw : nlines - 1;
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = make_float2(__ldg(x + line * NL + t + T * e), 0.f);
+  block_fft<NL, E, kFwd, 1, true>(v, s_x + q * XS, t, tw, 1);
+  if (valid) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) g[line * NL + t + T * e] = v[e];
+  }
+}
+
+// Adjoint of the reads of the coarse half spectrum by k_nufft_prep (inv_psi: its
+// deconvolution factors) or by k_dft_interp (inv_psi == nullptr: factors 1): the box
+// mode k in [-c/2, c/2 - 1]^dim reads Hh(k) for a half-axis frequency >= 0 and
+// conj Hh(-k) below, so
+//   Hb(q) = scale ([q_h <= c/2 - 1] s(k1) G(k1) + [q_h >= 1] s(k2) conj G(k2)),
+//   k1 = (cf(q_x), [cf(q_y),] q_h), k2 = (cf(-q_x), [cf(-q_y),] -q_h),
+// G on a gn^dim grid in fftfreq order (index k mod gn), cf: the frequency in [-c/2, c/2).
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_box_to_half_adj(const float2* __restrict__ G, long long gcs, int gn, int c, const float* __restrict__ inv_psi,
+                  float scale, float2* __restrict__ hb, long long hcs) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (i >= hcs) return;
+  const int hc = c / 2 + 1;
+  const int qh = (int)(i % hc);
+  const int qy = DIM == 3 ? (int)((i / hc) % c) : 0;
+  const int qx = DIM == 3 ? (int)(i / ((long long)hc * c)) : (int)(i / hc);
+  const float2* g = G + comp * gcs;
+  auto cf = [c](int v) { return v < c / 2 ? v : v - c; };
+  auto gidx = [gn](int k) { return (k % gn + gn) % gn; };
+  auto sfac = [&](int kx, int ky, int kh) {
+    if (!inv_psi) return 1.f;
+    const float sx = inv_psi[kx + c / 2], sh = inv_psi[kh + c / 2];
+    return DIM == 3 ? sx * inv_psi[ky + c / 2] * sh : sx * sh;
+  };
+  float2 acc = make_float2(0.f, 0.f);
+  if (qh <= c / 2 - 1) {
+    const int kx = cf(qx), ky = DIM == 3 ? cf(qy) : 0, kh = qh;
+    const long long o = DIM == 3 ? ((long long)gidx(kx) * gn + gidx(ky)) * gn + gidx(kh) : (long long)gidx(kx) * gn + gidx(kh);
+    const float s = sfac(kx, ky, kh);
+    acc.x += s * g[o].x;
+    acc.y += s * g[o].y;
+  }
+  if (qh >= 1) {
+    const int kx = cf((c - qx) % c), ky = DIM == 3 ? cf((c - qy) % c) : 0, kh = -qh;
+    const long long o = DIM == 3 ? ((long long)gidx(kx) * gn + gidx(ky)) * gn + gidx(kh) : (long long)gidx(kx) * gn + gidx(kh);
+    const float s = sfac(kx, ky, kh);
+    acc.x += s * g[o].x;
+    acc.y -= s * g[o].y;
+  }
+  hb[comp * hcs + i] = make_float2(scale * acc.x, scale * acc.y);
+}
+
+// The coarse real-field cotangent v = c^d irfftn_c(Hb / w) (w: half-axis multiplicity,
+// the adjoint of rfftn_c) seen through rfftn_c again: V = rfftn_c(v) = c^d P(Hb / w),
+// P the projection onto spectra of real fields, i.e. V = c^d Hb / 2 inside the half
+// axis and c^d (Hb(q) + conj Hb(q*)) / 2 on its planes 0 and c/2 (q* = (-q_x, [-q_y,]
+// q_h) mod c). k_uncrop_grad then maps V to the fine half spectrum (the adjoint of
+// spectral_filtering(irfftn(.)), the convention of the loss gradients).
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_herm_project(const float2* __restrict__ hb, long long hcs, int c, float cd, float2* __restrict__ V) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (i >= hcs) return;
+  const int hc = c / 2 + 1;
+  const int qh = (int)(i % hc);
+  const float2* h = hb + comp * hcs;
+  float2 v = h[i];
+  if (qh == 0 || qh == c / 2) {
+    const int qy = DIM == 3 ? (int)((i / hc) % c) : 0;
+    const int qx = DIM == 3 ? (int)(i / ((long long)hc * c)) : (int)(i / hc);
+    const int mx = (c - qx) % c, my = (c - qy) % c;
+    const long long m = DIM == 3 ? ((long long)mx * c + my) * hc + qh : (long long)mx * hc + qh;
+    const float2 w = h[m];
+    v = make_float2(v.x + w.x, v.y - w.y);
+  }
+  V[comp * hcs + i] = make_float2(0.5f * cd * v.x, 0.5f * cd * v.y);
+}
+
+// ------------------------------------------------------------------------------
 // Particle -> grid spectrum (turbulence.py:299-339, ur_to_u_dft_wrapper):
 // S_c(k) = sum_j u_r[j][c] exp(-i k . r_j) for every k of the N^dim grid in fftfreq
 // order. One thread per mode; particles streamed through shared memory in tiles of
@@ -487,6 +647,7 @@ struct l3es_interp_plan {
   double* rk_acc = nullptr;  // [np_max][dim] RK4 advection: velocity accumulator
   double* rk_pos = nullptr;  // [np_max][dim]   stage positions
   double* rk_vel = nullptr;  // [np_max][dim]   stage velocities
+  float2* hb = nullptr;      // [3][coarse half spectrum] interpolation adjoint
   l3es_plan* coarse = nullptr;  // size-c transforms (irfftn of Hh, rfftn of a coarse field)
   long long hcs = 0, gcs = 0;
   Ctx gctx;                  // geometry for the grid passes (twiddles only)
@@ -548,6 +709,35 @@ static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
   line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->g, p->gre, lines, p->tw, 1.0f);
 }
 
+// forward c2c passes of the real NUFFT grid gre (the adjoint of the inverse passes):
+// the contiguous axis (real -> complex, into g), then the strided axes in place
+template <int NG>
+static void grid_fwd_passes(const l3es_interp_plan* p, cudaStream_t s) {
+  using KY = KyCfg<NG>;
+  constexpr int TX = KY::THREADS, TWY = KY::TWY;
+  const long long per = p->gcs;
+  const long long lines = 3 * per / NG;
+  constexpr int LPC = (32 / Fft<NG>::T) * 4;
+  line_fft_real_fwd<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->gre, p->g, lines, p->tw);
+  if (p->dim == 3) {
+    ky_pass<NG, kFwd><<<dim3((NG + TWY - 1) / TWY, NG, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+    ky_pass<NG, kFwd><<<dim3((NG * NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
+  } else {
+    ky_pass<NG, kFwd><<<dim3((NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+  }
+}
+
+static int run_grid_fwd_passes(const l3es_interp_plan* p, cudaStream_t s) {
+  switch (p->n) {
+    case 16: grid_fwd_passes<16>(p, s); return L3ES_OK;
+    case 32: grid_fwd_passes<32>(p, s); return L3ES_OK;
+    case 64: grid_fwd_passes<64>(p, s); return L3ES_OK;
+    case 128: grid_fwd_passes<128>(p, s); return L3ES_OK;
+    case 256: grid_fwd_passes<256>(p, s); return L3ES_OK;
+    default: return fail(L3ES_EINVAL, "NUFFT grid size not supported");
+  }
+}
+
 static int run_grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
   switch (p->n) {
     case 16: grid_passes<16>(p, s); return L3ES_OK;
@@ -600,6 +790,7 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   rc = rc ? rc : ip_alloc(p, (void**)&p->rk_acc, rk_bytes, "rk4 accumulator");
   rc = rc ? rc : ip_alloc(p, (void**)&p->rk_pos, rk_bytes, "rk4 stage positions");
   rc = rc ? rc : ip_alloc(p, (void**)&p->rk_vel, rk_bytes, "rk4 stage velocities");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->hb, sizeof(float2) * 3 * p->hcs, "coarse spectrum adjoint");
   if (rc == L3ES_OK) {
     l3es_plan_desc d{};
     d.dim = dim;
@@ -777,17 +968,23 @@ int l3es_interp_advect_rk4(l3es_interp_plan* p, const double* r, int64_t np, dou
 
 // Fine NUFFT grid of the plan's coarse spectrum (deconvolve, zero-pad, 3 c2c passes, Re)
 // and the bin order of the positions r.
+static int bin_particles(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s);
+
 static int nufft_grid(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s) {
-  const unsigned pb = (unsigned)((np + 127) / 128);
   const unsigned gb = (unsigned)((p->gcs + 255) / 256);
   if (p->dim == 3)
     k_nufft_prep<3><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
   else
     k_nufft_prep<2><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
-  int rc = run_grid_passes(p, s);
-  if (rc != L3ES_OK) return rc;
+  const int rc = run_grid_passes(p, s);
+  return rc != L3ES_OK ? rc : bin_particles(p, r, np, s);
+}
+
+// counting sort of the particles by cell into p->perm
+static int bin_particles(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s) {
+  const unsigned pb = (unsigned)((np + 127) / 128);
   const int nbins = p->dim == 3 ? p->nb * p->nb * p->nb : p->nb * p->nb;
-  rc = cuda_check(cudaMemsetAsync(p->count, 0, sizeof(int) * nbins, s), "l3es_interp memset");
+  int rc = cuda_check(cudaMemsetAsync(p->count, 0, sizeof(int) * nbins, s), "l3es_interp memset");
   if (rc != L3ES_OK) return rc;
   if (p->dim == 3) {
     k_bin_count<3><<<pb, 128, 0, s>>>(r, np, p->nb, p->count);
@@ -802,6 +999,73 @@ static int nufft_grid(l3es_interp_plan* p, const double* r, int64_t np, cudaStre
 }
 
 extern "C" {
+
+int l3es_interp_vjp(l3es_interp_plan* p, const double* r, int64_t np, const double* lam, int32_t backend,
+                    void* grad_fine, void* stream) {
+  if (!p || !r || !lam || !grad_fine) return fail(L3ES_EINVAL, "l3es_interp_vjp: null argument");
+  if (p->n_fine <= 0) return fail(L3ES_ESTATE, "l3es_interp_vjp: plan was created without a fine grid (n_fine = 0)");
+  if (np < 0 || np > p->np_max) return fail(L3ES_EINVAL, "l3es_interp_vjp: np outside [0, np_max]");
+  if (backend != 0 && backend != 1) return fail(L3ES_EINVAL, "l3es_interp_vjp: backend must be 0 (nufft) or 1 (dft)");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int N = p->n_fine, c = p->c, dim = p->dim;
+  const long long cs = dim == 3 ? (long long)N * N * (N / 2 + 1) : (long long)N * (N / 2 + 1);
+  int rc = L3ES_OK;
+  if (np == 0) return cuda_check(cudaMemsetAsync(grad_fine, 0, sizeof(float2) * 3 * cs, s), "l3es_interp_vjp memset");
+  const unsigned hbk = (unsigned)((p->hcs + 255) / 256);
+  if (backend == 1) {
+    // S(k) = sum_j lam_j exp(-i k.r_j) on the c-grid (into p->g), then / c^dim
+    const long long modes = dim == 3 ? (long long)c * c * c : (long long)c * c;
+    const size_t smem = sizeof(float2) * 128 * dim * c;
+    if (smem > 200 * 1024) return fail(L3ES_EINVAL, "l3es_interp_vjp: ckp_N too large for the dft backend");
+    const float scale = (float)(1.0 / (double)modes);
+    if (dim == 3) {
+      cudaFuncSetAttribute(k_p2g_dft<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_p2g_dft<3><<<(unsigned)((modes + 127) / 128), 128, smem, s>>>(r, lam, np, 3, c, p->g, modes);
+      k_box_to_half_adj<3><<<dim3(hbk, 3), 256, 0, s>>>(p->g, modes, c, c, nullptr, scale, p->hb, p->hcs);
+    } else {
+      cudaFuncSetAttribute(k_p2g_dft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_p2g_dft<2><<<(unsigned)((modes + 127) / 128), 128, smem, s>>>(r, lam, np, 2, c, p->g, modes);
+      k_box_to_half_adj<2><<<dim3(hbk, 3), 256, 0, s>>>(p->g, modes, c, c, nullptr, scale, p->hb, p->hcs);
+    }
+  } else {
+    rc = bin_particles(p, r, np, s);
+    if (rc == L3ES_OK) rc = cuda_check(cudaMemsetAsync(p->gre, 0, sizeof(float) * 3 * p->gcs, s), "l3es_interp_vjp memset");
+    if (rc != L3ES_OK) return rc;
+    const double norm = 1.0 / (std::pow((double)p->n, dim) * std::pow((double)c, dim));
+    const float beta = (float)p->beta;
+    const unsigned gblk = (unsigned)((np * kGatherLanes + 127) / 128);
+#define L3ES_SPREAD(D, W) \
+  k_nufft_spread<D, W><<<gblk, 128, 0, s>>>(p->gre, p->gcs, p->n, dim, beta, norm, r, p->perm, np, lam)
+    if (dim == 3) {
+      if (p->w == 6) L3ES_SPREAD(3, 6);
+      else if (p->w == 8) L3ES_SPREAD(3, 8);
+      else L3ES_SPREAD(3, 4);
+    } else {
+      if (p->w == 6) L3ES_SPREAD(2, 6);
+      else if (p->w == 8) L3ES_SPREAD(2, 8);
+      else L3ES_SPREAD(2, 4);
+    }
+#undef L3ES_SPREAD
+    rc = run_grid_fwd_passes(p, s);
+    if (rc != L3ES_OK) return rc;
+    if (dim == 3)
+      k_box_to_half_adj<3><<<dim3(hbk, 3), 256, 0, s>>>(p->g, p->gcs, p->n, c, p->inv_psi, 1.f, p->hb, p->hcs);
+    else
+      k_box_to_half_adj<2><<<dim3(hbk, 3), 256, 0, s>>>(p->g, p->gcs, p->n, c, p->inv_psi, 1.f, p->hb, p->hcs);
+  }
+  // coarse cotangent -> fine half spectrum (p->g is free again: V goes there)
+  const float cd = (float)std::pow((double)c, dim);
+  const float uscale = (float)(0.5 / std::pow((double)N, dim));
+  const dim3 gb((unsigned)((cs + 255) / 256), 3);
+  if (dim == 3) {
+    k_herm_project<3><<<dim3(hbk, 3), 256, 0, s>>>(p->hb, p->hcs, c, cd, p->g);
+    k_uncrop_grad<3><<<gb, 256, 0, s>>>(p->g, p->hcs, c, N, cs, 3, uscale, (float2*)grad_fine);
+  } else {
+    k_herm_project<2><<<dim3(hbk, 3), 256, 0, s>>>(p->hb, p->hcs, c, cd, p->g);
+    k_uncrop_grad<2><<<gb, 256, 0, s>>>(p->g, p->hcs, c, N, cs, 2, uscale, (float2*)grad_fine);
+  }
+  return cuda_check(cudaGetLastError(), "l3es_interp_vjp launch");
+}
 
 int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const double* u_r, int64_t np,
                                   float* u_grid, void* stream) {

@@ -393,7 +393,7 @@ const char* l3es_kernel_kind_name(int32_t kind) { return kernel_kind_name(kind);
 }  // extern "C"
 
 // per-block partial sums of w |u_hat|^2 into c.partial ([batch][nblk]); returns nblk
-static int energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {
+int l3es::energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {
   // 8 blocks of 256 threads per SM of a 152-SM GB300, fewer when the field is small
   const int nblk = (int)std::min<long long>(std::min<long long>(c.npartial, 8 * 152), (3 * c.cs / 2 + 255) / 256);
   L3ES_LAUNCH(c, KK_REDUCE, 8.0 * 3.0 * c.cs * c.batch, s,

@@ -55,6 +55,7 @@ _SIGNATURES = {
     "l3es_interp_coarse_spectrum": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
     "l3es_interp_advect_rk4": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, ctypes.c_double, _P, _P]),
+    "l3es_interp_vjp": (ctypes.c_int, [_P, _P, ctypes.c_int64, _P, _I, _P, _P]),
     "l3es_shift": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P, _P]),
     "l3es_interp_particles_to_grid": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P]),
     "l3es_interp_dft_noalloc": (ctypes.c_int, [_I, _I, _I, _P, _P, ctypes.c_int64, _P, _P]),
@@ -390,6 +391,20 @@ class InterpPlan:
                 raise ValueError(f"positions and velocities are float64 (np, {self.dim})")
         _check(self._lib.l3es_interp_advect_rk4(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend],
                                                 float(dt), _ptr(r_out), _stream(stream)), "l3es_interp_advect_rk4")
+
+    def interp_vjp(self, r, lam, grad_fine, backend: str = "nufft", stream=None) -> None:
+        """grad_fine <- dL/du_hat_fine for the velocities of set_spectrum(u_hat_fine) +
+        interp(r) at fixed positions r, given lam = dL/du_r (float64 (np, dim))."""
+        import torch
+
+        if r.dtype != torch.float64 or lam.dtype != torch.float64 or r.shape != lam.shape or r.shape[-1] != self.dim:
+            raise ValueError(f"positions and cotangents are float64 (np, {self.dim})")
+        n = self.n_fine
+        want = 3 * n ** (self.dim - 1) * (n // 2 + 1)
+        if grad_fine.dtype != torch.complex64 or grad_fine.numel() != want:
+            raise ValueError(f"grad_fine must be a complex64 fine half spectrum of {want} values")
+        _check(self._lib.l3es_interp_vjp(self._h, _ptr(r), int(r.shape[0]), _ptr(lam), BACKENDS[backend],
+                                         _ptr(grad_fine), _stream(stream)), "l3es_interp_vjp")
 
     def coarse_mse(self, u_hat_fine, target, loss, grad=None, stream=None) -> None:
         """loss[0] = mean((spectral_filtering(irfftn(u_hat_fine), c) - target)^2) and,

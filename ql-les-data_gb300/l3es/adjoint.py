@@ -14,7 +14,10 @@ complex half spectra follow PyTorch's convention (dL/dRe + i dL/dIm).
     loss.backward()                       # u_hat0.grad
 
 ``loss_and_grad`` gives the same numbers without autograd bookkeeping. Supported
-forcings: none and const_power (ekin_tot rescaling is not differentiated).
+forcings: none, const_power and ekin_tot (its kinetic-energy rescaling after each step
+is differentiated too). ``interp`` differentiates the particle velocities of the
+combined loop (coarsening + NUFFT or exact DFT interpolation at fixed positions), so a
+loss on particle velocities reaches the initial spectrum through ``integrate``.
 """
 
 from __future__ import annotations
@@ -22,15 +25,16 @@ from __future__ import annotations
 from . import _native
 from .spectral_solver import _torch
 
-FORCING = {"none": "none", "const_power": "const_power"}
+FORCING = {"none": "none", "const_power": "const_power", "ekin_tot": "ekin_tot"}
 
 
-def make_plan(N, nu, dim, dt, forcing_type="none", kf=0, eps_inj=0.0, drag=0.0, batch=1):
-    """A step plan whose adjoint is available (forcing none or const_power)."""
+def make_plan(N, nu, dim, dt, forcing_type="none", kf=0, eps_inj=0.0, drag=0.0, batch=1, e_kin_init=0.0):
+    """A step plan whose adjoint is available (forcing none, const_power or ekin_tot;
+    the explicit viscous scheme)."""
     if forcing_type not in FORCING:
-        raise ValueError("differentiable forcings: 'none', 'const_power'")
+        raise ValueError("differentiable forcings: 'none', 'const_power', 'ekin_tot'")
     p = _native.Plan(dim=dim, n=N, nu=nu, dt=dt, forcing=forcing_type, kf=kf or 0, eps_inj=eps_inj,
-                     drag=drag, batch=batch)
+                     drag=drag, batch=batch, e_kin_init=e_kin_init)
     p.adjoint_prepare()
     return p
 
@@ -80,7 +84,28 @@ def _fn_classes():
             (g,) = ctx.saved_tensors
             return g * grad_loss.to(g.real.dtype), None, None
 
-    return Trajectory, CoarseMSE
+    class Interp(torch.autograd.Function):
+        """u_hat (fine half spectrum) -> particle velocities u_r at fixed positions r
+        (spectral_filtering to the plan's coarse grid, then NUFFT or exact DFT
+        interpolation, integrator.py:36-91); the backward pass is l3es_interp_vjp."""
+
+        @staticmethod
+        def forward(ctx, u_hat, r, iplan, backend):
+            u_r = torch.empty(r.shape, dtype=torch.float64, device=r.device)
+            iplan.set_spectrum(u_hat.detach().contiguous())
+            iplan.interp(r, u_r, backend=backend)
+            ctx.iplan, ctx.backend, ctx.shape = iplan, backend, u_hat.shape
+            ctx.save_for_backward(r)
+            return u_r
+
+        @staticmethod
+        def backward(ctx, grad_u_r):
+            (r,) = ctx.saved_tensors
+            g = torch.empty(ctx.shape, dtype=torch.complex64, device=r.device)
+            ctx.iplan.interp_vjp(r, grad_u_r.detach().to(torch.float64).contiguous(), g, backend=ctx.backend)
+            return g, None, None, None
+
+    return Trajectory, CoarseMSE, Interp
 
 
 _CLASSES = None
@@ -101,6 +126,17 @@ def integrate(u_hat0, plan, nsteps):
 def coarse_mse(u_hat, target, iplan):
     """Differentiable coarse-grid MSE loss (0-d float64 tensor)."""
     return _classes()[1].apply(u_hat, target, iplan)
+
+
+def particle_plan(dim, N, c, np_max, width=6):
+    """Interpolation plan for particle losses (coarsening from N to c, np_max particles)."""
+    return _native.InterpPlan(dim=dim, ckp_n=c, n_fine=N, width=width, np_max=np_max)
+
+
+def interp(u_hat, r, iplan, backend="nufft"):
+    """Differentiable particle velocities (np, dim) float64 at fixed positions r from the
+    fine half spectrum u_hat (torch.autograd; positions get no gradient)."""
+    return _classes()[2].apply(u_hat, r, iplan, backend)
 
 
 def loss_and_grad(u_hat0, plan, nsteps, target, iplan, checkpoints=None):

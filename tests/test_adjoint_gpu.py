@@ -129,11 +129,41 @@ def test_autograd_matches_direct_sweep():
     assert torch.equal(x.grad, g2)
 
 
-def test_ekin_tot_has_no_adjoint():
+@pytest.mark.parametrize("dim,n,kf", [(3, 32, 2), (2, 64, 3)])
+def test_ekin_tot_adjoint_step_matches_oracle(dim, n, kf):
+    """The adjoint of the step with ekin_tot forcing (the RK4 reverse sweep after the
+    adjoint of the kinetic-energy rescaling, spectral_solver.py:82-112) vs the FP64
+    oracle (ekin_tot_vjp, then rk4_step_vjp), with E0 below the current energy so the
+    rescaling is active."""
     from l3es import _native
 
-    p = _native.Plan(dim=3, n=16, nu=1e-2, dt=1e-3, forcing="ekin_tot", kf=2, e_kin_init=0.5)
-    with pytest.raises(RuntimeError, match="ekin_tot"):
+    nu, dt = 5e-3, 2e-3
+    uh = _state(dim, n, 17)
+    axes, rhs, vjp = _oracle_fns(dim, n, nu, 0.0, False)
+    _, kkk2, _, _ = R.wavenumbers(n, dim)
+    mask = ((kkk2 > 0) & (kkk2 <= kf * kf)).astype(float)
+    e_all = A.ekin_tot_forward(uh, mask, 0.0, n, dim)
+    e0 = 0.95 * (e_all[2] + e_all[3])
+    u_rk = A.rk4_step(uh, dt, rhs)
+    lam = _crand(uh.shape, 18, dim)
+    ref = A.rk4_step_vjp(uh, A.ekin_tot_vjp(u_rk, lam, mask, e0, n, dim), dt, rhs, vjp)
+    plan = _native.Plan(dim=dim, n=n, nu=nu, dt=dt, forcing="ekin_tot", kf=kf, e_kin_init=e0)
+    plan.adjoint_prepare()
+    u0 = _c64(uh)
+    got = _c64(lam)
+    plan.adjoint_step(u0, got)
+    assert _rel(got, ref) < 3e-5
+    # the forward step agrees with the oracle's rescaled step too (same e0, same state)
+    fw = _c64(uh)
+    plan.step(fw, 1)
+    assert _rel(fw, A.ekin_tot_forward(u_rk, mask, e0, n, dim)[0]) < 2e-5
+
+
+def test_integrating_factor_plans_have_no_adjoint():
+    from l3es import _native
+
+    p = _native.Plan(dim=3, n=16, nu=1e-2, dt=1e-3, scheme="integrating_factor")
+    with pytest.raises(RuntimeError, match="explicit"):
         p.adjoint_prepare()
 
 
@@ -212,3 +242,80 @@ def test_batched_adjoint_matches_single_plans():
     got = lam_b.cpu().numpy()
     for b in range(2):
         assert np.abs(got[b] - singles[b]).max() <= 1e-6 * np.abs(singles[b]).max()
+
+
+@pytest.mark.parametrize("dim,n,c,np_", [(3, 32, 16, 600), (2, 64, 32, 900)])
+def test_interp_vjp_matches_oracle_and_finite_differences(dim, n, c, np_):
+    """Adjoint of the particle interpolation (coarsening + NUFFT / exact DFT at fixed
+    positions) vs the FP64 oracle VJP of interpolate_dft, and its directional
+    derivatives vs central differences of the FP64 forward oracle (1e-4)."""
+    from l3es import adjoint as AD
+
+    axes = (1, 2, 3) if dim == 3 else (1, 2)
+    uh = _state(dim, n, 3)
+    if dim == 2:
+        uh = uh.reshape(3, n, n // 2 + 1)
+    rng = np.random.default_rng(9)
+    r = rng.uniform(0, 2 * np.pi, (np_, dim))
+    lam = rng.standard_normal((np_, dim))
+    ref = A.interp_vjp(lam, r, n, c, axes)
+    ip = AD.particle_plan(dim, n, c, np_)
+    rt = torch.from_numpy(r).cuda()
+    lt = torch.from_numpy(lam).cuda()
+
+    def loss64(u_hat):
+        return float(np.sum(lam * R.interpolate_from_uhat_dft(u_hat, n, c, r, dim)))
+
+    for backend, tol in (("dft", 2e-5), ("nufft", 1e-4)):
+        g = torch.empty(uh.shape, dtype=torch.complex64, device="cuda")
+        ip.interp_vjp(rt, lt, g, backend=backend)
+        torch.cuda.synchronize()
+        assert _rel(g, ref) < tol, backend
+        gn = g.cpu().numpy().astype(np.complex128)
+        h = 1e-3
+        for k in range(3):
+            x = np.random.default_rng(100 + k).standard_normal((3,) + (n,) * dim)
+            if dim == 2:
+                x[2] = 0.0
+            d = np.fft.rfftn(x, axes=axes) * (np.abs(uh).max() / n**dim)
+            fd = (loss64(uh + h * d) - loss64(uh - h * d)) / (2 * h)
+            ad = float(np.real(np.sum(np.conj(gn) * d)))
+            assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-12), (backend, ad, fd)
+    # autograd through the interpolation gives the same gradient
+    u = _c64(uh).requires_grad_(True)
+    ur = AD.interp(u, rt, ip, backend="nufft")
+    (ur * lt).sum().backward()
+    assert _rel(u.grad, ref) < 1e-4
+
+
+def test_particle_loss_gradient_through_the_step():
+    """A loss on particle velocities after 3 RK4 steps differentiates back to the
+    initial half spectrum (adjoint steps + interpolation adjoint, autograd), vs central
+    differences of the FP64 oracle trajectory (1e-4)."""
+    from l3es import adjoint as AD
+
+    n, c, np_, nu, dt, steps = 32, 16, 500, 0.01, 5e-3, 3
+    uh = _state(3, n, 4)
+    rng = np.random.default_rng(10)
+    r = rng.uniform(0, 2 * np.pi, (np_, 3))
+    lam = rng.standard_normal((np_, 3))
+    plan = AD.make_plan(n, nu, 3, dt)
+    ip = AD.particle_plan(3, n, c, np_)
+    u = _c64(uh).requires_grad_(True)
+    ur = AD.interp(AD.integrate(u, plan, steps), torch.from_numpy(r).cuda(), ip, backend="dft")
+    (ur * torch.from_numpy(lam).cuda()).sum().backward()
+    g = u.grad.cpu().numpy().astype(np.complex128)
+    rhs = R.rhs_wrapper(n, nu)
+
+    def loss64(u_hat):
+        for _ in range(steps):
+            u_hat = A.rk4_step(u_hat, dt, rhs)
+        return float(np.sum(lam * R.interpolate_from_uhat_dft(u_hat, n, c, r)))
+
+    h = 1e-3
+    for k in range(3):
+        x = np.random.default_rng(200 + k).standard_normal((3, n, n, n))
+        d = np.fft.rfftn(x, axes=(1, 2, 3)) * (np.abs(uh).max() / n**3)
+        fd = (loss64(uh + h * d) - loss64(uh - h * d)) / (2 * h)
+        ad = float(np.real(np.sum(np.conj(g) * d)))
+        assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-12), (ad, fd)

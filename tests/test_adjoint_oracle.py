@@ -90,3 +90,70 @@ def test_fp64_torch_restatement_equals_numpy_oracle():
     l1, g1 = M.loss_and_grad(t, 2, torch.from_numpy(tgt))
     l2, g2 = A.trajectory_loss_and_grad(uh, 2, 2e-3, rhs, vjp, tgt, 8)
     assert abs(l1 - l2) < 1e-13 * l2 and rel(g1, g2) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_interp_vjp_matches_finite_differences(dim):
+    """The FP64 adjoint of the particle interpolation (coarsening to c, then the exact
+    spectral interpolation at fixed positions) against central differences of the
+    forward oracle (interpolate_from_uhat_dft) along random directions."""
+    rng, axes, uh, mask, crand = _setup(dim, 21)
+    c, npart = 8, 40
+    r = rng.uniform(0, 2 * np.pi, (npart, dim))
+    lam = rng.standard_normal((npart, dim))
+
+    def loss(u_hat):
+        return float(np.sum(lam * R.interpolate_from_uhat_dft(u_hat, N, c, r, dim)))
+
+    g = A.interp_vjp(lam, r, N, c, axes)
+    assert g.shape == uh.shape
+    h = 1e-4
+    for _ in range(4):
+        d = crand()
+        fd = (loss(uh + h * d) - loss(uh - h * d)) / (2 * h)
+        ad = float(np.real(np.sum(np.conj(g) * d)))
+        assert abs(ad - fd) <= 1e-8 * max(1.0, abs(fd)), (ad, fd)
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_ekin_tot_vjp_matches_finite_differences(dim):
+    """The FP64 adjoint of the ekin_tot rescaling (spectral_solver.py:82-112) against
+    central differences of its Parseval form, and the whole forced RK4 step
+    (rk4_step_vjp after ekin_tot_vjp) against the reference restatement's step
+    (rk4_wrapper with forcing_type 'ekin_tot'), along spectra of real fields."""
+    rng, axes, uh, mask, crand = _setup(dim, 31)
+    e0 = 0.8 * A.ekin_tot_forward(uh, mask, 0.0, N, dim)[2] + 0.5 * A.ekin_tot_forward(uh, mask, 0.0, N, dim)[3]
+    lam = crand()
+    g = A.ekin_tot_vjp(uh, lam, mask, e0, N, dim)
+
+    def real_dir(seed):
+        x = np.random.default_rng(seed).standard_normal((3,) + (N,) * dim)
+        if dim == 2:
+            x[2] = 0.0
+        return np.fft.rfftn(x, axes=axes) * np.abs(uh).max() / N**dim
+
+    h = 1e-4
+    for k in range(3):
+        d = real_dir(k)
+        lp = float(np.real(np.sum(np.conj(lam) * A.ekin_tot_forward(uh + h * d, mask, e0, N, dim)[0])))
+        lm = float(np.real(np.sum(np.conj(lam) * A.ekin_tot_forward(uh - h * d, mask, e0, N, dim)[0])))
+        fd = (lp - lm) / (2 * h)
+        ad = float(np.real(np.sum(np.conj(g) * d)))
+        assert abs(ad - fd) <= 1e-7 * max(1.0, abs(fd)), (ad, fd)
+    # the forced step: the reference restatement's rk4_wrapper(..., "ekin_tot")
+    nu, dt = 0.01, 0.01
+    rhs = R.rhs_wrapper(N, nu, axes)
+    vjp = A.rhs_vjp_wrapper(N, nu, axes)
+    step = R.rk4_wrapper(dt, rhs, mask, e0, "ekin_tot", axes)
+    def phys(x):  # the step's first stage reads the caller's u = irfftn(u_hat)
+        x = np.fft.irfftn(x, axes=axes)
+        return x[..., None] if dim == 2 else x
+
+    u_rk = A.rk4_step(uh, dt, rhs)
+    gs = A.rk4_step_vjp(uh, A.ekin_tot_vjp(u_rk, lam, mask, e0, N, dim), dt, rhs, vjp)
+    for k in range(2):
+        d = real_dir(10 + k)
+        up, um = step(phys(uh + h * d), uh + h * d)[1], step(phys(uh - h * d), uh - h * d)[1]
+        fd = float(np.real(np.sum(np.conj(lam) * (up - um)))) / (2 * h)
+        ad = float(np.real(np.sum(np.conj(gs) * d)))
+        assert abs(ad - fd) <= 1e-6 * max(1.0, abs(fd)), (ad, fd)
