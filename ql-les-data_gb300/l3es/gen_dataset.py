@@ -186,10 +186,13 @@ def compute_statistics_h5(args) -> dict:
         aus.append((uu[1:] - uu[:-1]).mean((0, 1)))
     vel_mean, acc_mean = np.stack(vs).mean(0), np.stack(avs).mean(0)
     u_mean, au_mean = np.stack(us).mean(0), np.stack(aus).mean(0)
+    # As the reference computes them: its velocity and acceleration spreads are taken
+    # about 0, because the centring values it subtracts (v_mean, av_mean) are set to 0.0
+    # and never updated (gen_dataset.py:157, :180-183); u and au are centred on their means.
     v_sq, av_sq, u_sq, au_sq = [], [], [], []
     for vel, uu in fields():
-        v_sq.append(np.square(vel - vel_mean).mean((0, 1)))
-        av_sq.append(np.square(vel[1:] - vel[:-1] - acc_mean).mean((0, 1)))
+        v_sq.append(np.square(vel).mean((0, 1)))
+        av_sq.append(np.square(vel[1:] - vel[:-1]).mean((0, 1)))
         u_sq.append(np.square(uu - u_mean).mean((0, 1)))
         au_sq.append(np.square(uu[1:] - uu[:-1] - au_mean).mean((0, 1)))
     stds = [np.stack(a).mean(0) ** 0.5 for a in (v_sq, av_sq, u_sq, au_sq)]

@@ -53,8 +53,10 @@ def _stats_oracle(trajs, every):
     for name, arrs in (("vel", vels), ("u", us)):
         m = np.mean([a.mean((0, 1)) for a in arrs], axis=0)
         am = np.mean([(a[1:] - a[:-1]).mean((0, 1)) for a in arrs], axis=0)
-        sd = np.mean([np.square(a - m).mean((0, 1)) for a in arrs], axis=0) ** 0.5
-        asd = np.mean([np.square(a[1:] - a[:-1] - am).mean((0, 1)) for a in arrs], axis=0) ** 0.5
+        # the reference's velocity / acceleration spreads are about 0 (gen_dataset.py:157)
+        c, ac = (m, am) if name == "u" else (0.0, 0.0)
+        sd = np.mean([np.square(a - c).mean((0, 1)) for a in arrs], axis=0) ** 0.5
+        asd = np.mean([np.square(a[1:] - a[:-1] - ac).mean((0, 1)) for a in arrs], axis=0) ** 0.5
         out[name] = (m, sd, am, asd)
     return out
 
@@ -141,3 +143,46 @@ def test_kolm_init_matches_oracle_and_is_solenoidal(N, G):
     assert full.shape == (2, G, G, 1)
     assert abs(np.sqrt((full[..., 0] ** 2).sum(0)).max() - 4.2) < 1e-12
     assert not np.array_equal(u, F.init_u_kolm(N, seed=6, grid_n=G))
+
+
+@pytest.mark.parametrize("case", ["plain", "sliced", "statsliced"])
+def test_dataset_matches_reference_golden(tmp_path, case):
+    """The same trajectories through the reference's own gen_dataset.py (run with
+    stand-ins for h5py, omegaconf and jax_sph's io and periodic space; see
+    tests/golden/make_golden_dataset.py) and through l3es.gen_dataset: identical split
+    contents, metadata and statistics."""
+    z = np.load(os.path.join(HERE, "golden", "gen_dataset.npz"))
+    g = {k.split(":", 1)[1]: z[k] for k in z.files if k.startswith(case + ":")}
+    cfg = json.loads(str(g["config"]))
+    src, dst = tmp_path / "raw", tmp_path / "ds"
+    for s in g["seeds"]:
+        com = src / f"traj_{s}" / "com"
+        com.mkdir(parents=True)
+        r, u = g[f"in_r_{s}"], g[f"in_u_{s}"]
+        for k in range(r.shape[0]):
+            np.savez(com / f"step_{k * cfg['com']['ckp_freq']:05d}.npz", r=r[k], u=u[k])
+        (src / f"traj_{s}" / "config.json").write_text(json.dumps(cfg))
+    GD.main(["--src_dir", str(src), "--dst_dir", str(dst), "--split", str(g["split"]),
+             "--skip_first_n_frames", str(int(g["skip"])), "--slice_every_nth_frame", str(int(g["slice"])),
+             "--stats_every_nth", str(int(g["stats"]))])
+    ext = ".h5" if GD.h5py is not None else ".npz"
+    for split in ("train", "valid", "test"):
+        got = list(GD._read_split(str(dst / f"{split}{ext}")))
+        keys = sorted({k.split("/")[1] for k in g if k.startswith(f"out_{split}/")})
+        assert len(got) == len(keys)
+        for (ptype, pos, u), key in zip(got, keys):
+            np.testing.assert_array_equal(ptype, g[f"out_{split}/{key}/particle_type"])
+            np.testing.assert_array_equal(pos, g[f"out_{split}/{key}/position"])
+            np.testing.assert_array_equal(u, g[f"out_{split}/{key}/u"])
+    meta = json.loads((dst / "metadata.json").read_text())
+    ref_meta = json.loads(str(g["metadata"]))
+    assert meta == ref_meta
+    n = int(g["stats"])
+    stats = json.loads((dst / f"metadata_every{n}.json").read_text())
+    ref_stats = json.loads(str(g["metadata_stats"]))
+    assert stats.keys() == ref_stats.keys()
+    for k, v in ref_stats.items():
+        if k.endswith(("_mean", "_std")):
+            np.testing.assert_allclose(stats[k], v, rtol=2e-6, atol=1e-7)
+        else:
+            assert stats[k] == v, k
