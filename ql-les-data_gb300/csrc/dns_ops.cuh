@@ -104,7 +104,7 @@ struct DnsOps {
       const long long cap = line2_ctas > 0 ? std::max(1, line2_ctas / c.batch) : tiles;
       L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
                   line_cross2<N><<<dim3((unsigned)std::min(tiles, cap), c.batch), L2::THREADS, 0, s>>>(
-                      c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines));
+                      c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines, c.work));
     } else {
       L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
                   line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(

@@ -145,6 +145,7 @@ struct Ctx {
   double* einj = nullptr;      // [batch] scratch e_inj
   float* nu_b = nullptr;       // [batch] viscosity per trajectory
   int* err = nullptr;          // device error word: nonzero after a kernel wait timed out
+  unsigned* work = nullptr;    // [batch][2] work counters of the persistent line pass (zero between launches)
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate
   KTimer* timer = nullptr;     // per-launch timing (nullptr = off)

@@ -98,12 +98,10 @@ static float2 twiddle(long long m, long long n) {
   return make_float2((float)std::cos(a), (float)std::sin(a));
 }
 
-// FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n), followed by the compact
-// per-stage table of the n/2-point line FFT (radix-8 schedule; Sched::ctoff layout):
-// for stage s >= 1 of radix R with Ns points per sub-transform, entries r = 1..R-1,
-// jm = 0..Ns-1 hold exp(-2 pi i r jm / (Ns R)). Same FP64 angles (scaled by powers of
-// two) as the strided table, so both give the same FP32 values.
-// Appends the compact per-stage table of an m-point FFT (radix-8 schedule).
+// Appends the compact per-stage table of an m-point FFT (radix-8 schedule; Sched::ctoff
+// layout): for stage s >= 1 of radix R with Ns points per sub-transform, entries
+// r = 1..R-1, jm = 0..Ns-1 hold exp(-2 pi i r jm / (Ns R)). Same FP64 angles (scaled by
+// powers of two) as the strided table, so both give the same FP32 values.
 static void push_compact_table(std::vector<float2>& t, int m) {
   const int E = m >= 8 ? 8 : m;
   std::vector<int> radix;
@@ -123,8 +121,9 @@ static void push_compact_table(std::vector<float2>& t, int m) {
   }
 }
 
-// ... followed by the compact table of the n-point FFT (the two-for-one line pass,
-// at line2_ct_offset<n>()).
+// FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n), followed by the compact
+// table of the n/2-point line FFT and that of the n-point FFT (the two-for-one line
+// pass, at line2_ct_offset<n>()).
 static std::vector<float2> twiddles(int n) {
   std::vector<float2> t(n);
   for (int m = 0; m < n; ++m) t[m] = twiddle(m, n);
@@ -265,6 +264,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");
   rc = rc ? rc : plan_alloc(p, (void**)&c.nu_b, sizeof(float) * B, "viscosities");
   rc = rc ? rc : plan_alloc(p, (void**)&c.err, sizeof(int), "error word");
+  rc = rc ? rc : plan_alloc(p, (void**)&c.work, sizeof(unsigned) * 2 * B, "work counters");
   if (rc != L3ES_OK) {
     plan_free(p);
     delete p;
@@ -277,6 +277,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
   if (e == cudaSuccess) e = cudaMemset(c.err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c.work, 0, sizeof(unsigned) * 2 * B);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     rc = cuda_check(e, "l3es_plan_create");

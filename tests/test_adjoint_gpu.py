@@ -263,8 +263,15 @@ def test_interp_vjp_matches_oracle_and_finite_differences(dim, n, c, np_):
     rt = torch.from_numpy(r).cuda()
     lt = torch.from_numpy(lam).cuda()
 
-    def loss64(u_hat):
-        return float(np.sum(lam * R.interpolate_from_uhat_dft(u_hat, n, c, r, dim)))
+    from oracle import nufft_ref as NU
+
+    def loss64(u_hat, backend):
+        # FP64 forward of the same backend: the exact DFT (integrator.py:62-91) or the
+        # restated type-2 NUFFT (ES kernel w = 6, sigma = 2), after spectral_filtering
+        if backend == "dft":
+            return float(np.sum(lam * R.interpolate_from_uhat_dft(u_hat, n, c, r, dim)))
+        u = np.fft.irfftn(u_hat, s=(n,) * dim, axes=axes)[:dim]
+        return float(np.sum(lam * NU.interpolate_nufft(R.spectral_filtering(u, c), r, w=6)))
 
     for backend, tol in (("dft", 2e-5), ("nufft", 1e-4)):
         g = torch.empty(uh.shape, dtype=torch.complex64, device="cuda")
@@ -278,7 +285,7 @@ def test_interp_vjp_matches_oracle_and_finite_differences(dim, n, c, np_):
             if dim == 2:
                 x[2] = 0.0
             d = np.fft.rfftn(x, axes=axes) * (np.abs(uh).max() / n**dim)
-            fd = (loss64(uh + h * d) - loss64(uh - h * d)) / (2 * h)
+            fd = (loss64(uh + h * d, backend) - loss64(uh - h * d, backend)) / (2 * h)
             ad = float(np.real(np.sum(np.conj(gn) * d)))
             assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-12), (backend, ad, fd)
     # autograd through the interpolation gives the same gradient
