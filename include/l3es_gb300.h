@@ -325,6 +325,16 @@ int l3es_sph_relax_velocity(l3es_sph_plan* plan, const double* r0, const double*
 typedef struct l3es_graph l3es_graph;
 int l3es_graph_begin(void** capture_stream);
 int l3es_graph_end(void* capture_stream, l3es_graph** out);
+
+/* Branches of a recording (no counterpart in the reference): l3es_graph_fork opens a
+ * stream that joins the recording of capture_stream (or of one of its branches); calls
+ * given it depend on what that stream had recorded so far and run concurrently with
+ * everything recorded elsewhere until l3es_graph_join, after which the capturing
+ * stream's later calls wait for the branch. Every fork must be joined before
+ * l3es_graph_end, which releases the branch streams. Trajectories of different grid
+ * sizes recorded on separate branches execute side by side in one graph launch. */
+int l3es_graph_fork(void* capture_stream, void** branch_stream);
+int l3es_graph_join(void* capture_stream, void* branch_stream);
 int l3es_graph_launch(l3es_graph* graph, void* stream);
 int l3es_graph_destroy(l3es_graph* graph);
 

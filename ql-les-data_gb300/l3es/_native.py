@@ -31,6 +31,8 @@ _SIGNATURES = {
     "l3es_graph_begin": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "l3es_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "l3es_graph_launch": (ctypes.c_int, [_P, _P]),
+    "l3es_graph_fork": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "l3es_graph_join": (ctypes.c_int, [_P, _P]),
     "l3es_graph_destroy": (ctypes.c_int, [_P]),
     "l3es_step": (ctypes.c_int, [_P, _P, _P, _I, _P, _P]),
     "l3es_step_energy": (ctypes.c_int, [_P, _P, _P, _I, _P, _P, _P]),
@@ -562,6 +564,18 @@ class Graph:
         h = ctypes.c_void_p()
         _check(load().l3es_graph_begin(ctypes.byref(h)), "l3es_graph_begin")
         return _CaptureStream(h.value)
+
+    @staticmethod
+    def fork(cap: _CaptureStream) -> _CaptureStream:
+        """A branch of the recording: calls given it run concurrently with the rest of
+        the recording until join(cap, branch)."""
+        h = ctypes.c_void_p()
+        _check(load().l3es_graph_fork(cap.cuda_stream, ctypes.byref(h)), "l3es_graph_fork")
+        return _CaptureStream(h.value)
+
+    @staticmethod
+    def join(cap: _CaptureStream, branch: _CaptureStream) -> None:
+        _check(load().l3es_graph_join(cap.cuda_stream, branch.cuda_stream), "l3es_graph_join")
 
     @staticmethod
     def end(cap: _CaptureStream) -> "Graph":
