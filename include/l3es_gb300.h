@@ -100,6 +100,23 @@ int l3es_plan_set_nu(l3es_plan* plan, const double* nu_host, int32_t count);
 /* Scratch bytes the plan holds on the device (for capacity planning). */
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
 
+/* Kernel schedule of the plan's step (no counterpart in the reference, whose XLA
+ * compiler picks its own kernels, spectral_solver.py:130-153): four 0/1 choices,
+ *   [0] 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA),
+ *   [1] y passes with the radix-8 schedule (else radix 16 from N = 128),
+ *   [2] the two-for-one half-axis line pass for 64 <= N <= 256 (else the packed one),
+ *   [3] the persistent bulk-copy band x pass (else one tile per CTA).
+ * Every schedule computes the same step; only speed differs. */
+int l3es_plan_get_schedule(const l3es_plan* plan, int32_t* sched4);
+int l3es_plan_set_schedule(l3es_plan* plan, const int32_t* sched4);
+
+/* Autotuner: times the plan's right-hand side on its own scratch under each schedule
+ * choice (one knob at a time) and keeps the fastest. cache_path (nullable) names a
+ * text file of earlier results, one line per GPU model, dim, N and batch; a hit skips
+ * the timing, a miss appends the result. Synchronises the stream; not while recording
+ * a graph. */
+int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void* stream);
+
 /* Diagnostics of the drivers, FP64 results on the device (per trajectory):
  * l3es_field_stats: out[4] = max|u_x|, max|u_y|, max|u_z|, 0.5 mean sum u^2 of a
  *   physical field (spectral_solver.py:318-319; comp_dt at :123-127 follows from the

@@ -50,11 +50,13 @@ struct LineCfg {
   static constexpr int PS = 3 * M + T;
 };
 
-// y-axis pass tiling: radix 16 (one exchange at N = 256) on 16-column tiles where the
-// shared-memory tile fits the static limit.
-template <int N>
+// y-axis pass tiling, two schedules (the plan's autotuner picks one per grid):
+//   V = 0: radix 16 from N = 128 (one exchange at N = 256), radix 8 below;
+//   V = 1: radix 8 throughout (two exchanges at N = 256, twice the threads per tile).
+// 16-column tiles where the shared-memory tile fits the static limit, else 8.
+template <int N, int V = 0>
 struct KyCfg {
-  static constexpr int E = N >= 128 ? 16 : Fft<N>::E;
+  static constexpr int E = (V == 0 && N >= 128) ? 16 : Fft<N>::E;
   static constexpr int TWY = (N >= 128 && N <= 256) ? 16 : 8;
   static constexpr int T = N / E;
   static constexpr int THREADS = TWY * T;
@@ -227,11 +229,11 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
 // columns [0, ncols). Only rows whose signed wavenumber satisfies |ky| <= kd_store
 // are written (forward pass truncated to the dealiased band; kd_store = N/2 keeps all).
 // ------------------------------------------------------------------------------
-template <int N, int DIR>
-__global__ void __launch_bounds__(KyCfg<N>::THREADS)
+template <int N, int DIR, int V = 0>
+__global__ void __launch_bounds__(KyCfg<N, V>::THREADS)
 ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
         const float2* __restrict__ tw) {
-  using C = KyCfg<N>;
+  using C = KyCfg<N, V>;
   constexpr int E = C::E, T = C::T, TWY = C::TWY;
   __shared__ float2 sm[xpad_len<TWY>(N) * TWY];
   const int p = threadIdx.x % TWY, t = threadIdx.x / TWY;
@@ -261,10 +263,10 @@ ky_pass(float2* __restrict__ w, long long fs, int row, int ncols, int kd_store,
 //          pass does not store it;
 //   jobs 4, 5: u_y, u_z from the side buffer wx (x-transformed W_y, W_z) -> fields 1, 2.
 // No job writes what another job reads.
-template <int N>
-__global__ void __launch_bounds__(KyCfg<N>::THREADS)
+template <int N, int V = 0>
+__global__ void __launch_bounds__(KyCfg<N, V>::THREADS)
 ky_inv_rhs(float2* __restrict__ w, const float2* __restrict__ wx, long long fs, const float2* __restrict__ tw) {
-  using C = KyCfg<N>;
+  using C = KyCfg<N, V>;
   constexpr int E = C::E, T = C::T, TWY = C::TWY, H = N / 2 + 1;
   __shared__ float2 sm[xpad_len<TWY>(N) * TWY];
   const int p = threadIdx.x % TWY, t = threadIdx.x / TWY;
@@ -568,19 +570,16 @@ __device__ __forceinline__ void prefetch_line6(const float2* src, long long fs, 
   }
 }
 
-// Persistent: each line slot (T lanes) takes line pairs (A, B), counted from the last
-// line, from a per-trajectory work counter (one atomic per pair: no tail imbalance
-// between slots), and prefetches into L1 the six input lines of the next line it will
-// transform (B while A runs, the next pair's A while B runs), so a pair's loads hit L1
-// instead of waiting on L2 / DRAM (the kernel's registers leave no room for a register
-// prefetch). The loops stay rolled: the inverse and the forward FFT code appear once,
-// which keeps the instruction footprint small for warps that drift apart.
-// work[batch * 2]: {next pair, finished CTAs}, zero on entry; the last CTA of each
-// trajectory to finish sets both back to zero for the next launch.
+// One line pair (A, B) per line slot, lines counted from the last; line B's six input
+// lines are prefetched into L1 while line A is transformed, so B's loads hit L1 instead
+// of waiting on L2 / DRAM (the kernel's registers leave no room for a register prefetch).
+// Measured alternatives, kept out: persistent slots walking many pairs with a prefetch of
+// each next line (144.7 vs 141.5 us at 256^3: the drifting warps miss the instruction
+// cache), the same with rolled loops and work counters (161 us: 22% more instructions).
 template <int N>
 __global__ void __launch_bounds__(Line2Cfg<N>::THREADS, 4)
 line_cross2(const float2* __restrict__ w, long long fs, float2* __restrict__ du, long long ds, int kt, int kd,
-            float s2, const float2* __restrict__ ct, int nlines, unsigned* __restrict__ work) {
+            float s2, const float2* __restrict__ ct, int nlines) {
   static_assert(N >= 64 && N <= 256, "two-for-one line pass: N in [64, 256]");
   using C = Line2Cfg<N>;
   constexpr int T = C::T, H = N / 2 + 1;
@@ -589,93 +588,59 @@ line_cross2(const float2* __restrict__ w, long long fs, float2* __restrict__ du,
   float2* xs = s_x + slot * C::XS;
   const float2* wb = w + (long long)blockIdx.y * 6 * fs;
   float2* db = du + (long long)blockIdx.y * 3 * ds;
-  unsigned* ctr = work + 2 * blockIdx.y;
-  const int npairs = (nlines + 1) / 2;
-  // a warp takes SPW consecutive pairs per grab (one per slot), so its slots loop in
-  // step and the full-warp shuffles of the FFTs stay converged
-  constexpr int SPW = 32 / T;
-  const int sw = (threadIdx.x & 31) / T;  // slot inside the warp
-  auto grab = [&]() {
-    unsigned v = 0;
-    if ((threadIdx.x & 31) == 0) v = atomicAdd(ctr, (unsigned)SPW);
-    return (int)__shfl_sync(0xffffffffu, v, 0);
-  };
-  auto line_of = [&](int idx) { return (long long)(nlines - 1 - idx); };
-  int base = grab();
-  int nbase = base < npairs ? grab() : npairs;
-  if (base + sw < npairs) prefetch_line6<N>(wb + line_of(2 * (base + sw)) * H, fs, t);
-  float pa[8];  // z component of u x curl u of line A
-#pragma unroll 1
-  while (base < npairs) {  // warp-uniform
-    const int pair = base + sw;
-    const bool pvalid = pair < npairs;
-#pragma unroll 1
-    for (int half = 0; half < 2; ++half) {
-      const int idx = 2 * pair + half;
-      const bool valid = pvalid && idx < nlines;
-      const long long line = valid ? line_of(idx) : nlines - 1;  // idle slots mirror a valid line
-      const int nxt = half == 0 ? idx + 1 : 2 * (nbase + sw);  // the line transformed after this one
-      if (pvalid && nxt < nlines) prefetch_line6<N>(wb + line_of(nxt) * H, fs, t);
-      const float2* src = wb + line * H;
-      float2 h1[8], h2[8], z[8];
-#pragma unroll 1
-      for (int pr = 0; pr < 3; ++pr) {  // (u_x, u_y), (u_z, curl_x), (curl_y, curl_z)
-        c2r_pair_load<N>(src + 2 * pr * fs, src + (2 * pr + 1) * fs, t, z);
-        warp_fft<N, 8, kInv>(z, xs, t, ct);
-        __syncwarp();
+  const long long ia = 2 * ((long long)blockIdx.x * C::SLOTS + slot);  // line A; B = A + 1
+  if (ia + 1 < nlines) prefetch_line6<N>(wb + (nlines - 2 - ia) * H, fs, t);
+  float pa[8], pb[8];  // z component of u x curl u of lines A and B
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          if (pr == 0) h1[e] = z[e];
-          if (pr == 1) h2[e] = z[e];
-        }
-      }
-      // u x curl u at this lane's positions (unnormalised: the scale enters in s2)
-      float pz[8];
+  for (int half = 0; half < 2; ++half) {
+    const long long idx = ia + half;
+    const bool valid = idx < nlines;
+    const long long line = valid ? nlines - 1 - idx : nlines - 1;  // idle slots mirror a valid line
+    const float2* src = wb + line * H;
+    float2 h1[8], h2[8], z[8];
+    c2r_pair_load<N>(src, src + fs, t, z);  // u_x + i u_y
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const float ux = h1[e].x, uy = h1[e].y, uz = h2[e].x, wx = h2[e].y, wy = z[e].x, wz = z[e].y;
-        pz[e] = fmaf(ux, wy, -uy * wx);
-        z[e] = make_float2(fmaf(uy, wz, -uz * wy), fmaf(uz, wx, -ux * wz));
-      }
-      // forward jobs: (x, y) of this line; after line B also (z of A, z of B)
-#pragma unroll 1
-      for (int fj = 0; fj < 1 + half; ++fj) {
-        if (fj == 1) {
+    for (int e = 0; e < 8; ++e) h1[e] = z[e];
+    __syncwarp();
+    c2r_pair_load<N>(src + 2 * fs, src + 3 * fs, t, z);  // u_z + i curl_x
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
 #pragma unroll
-          for (int e = 0; e < 8; ++e) z[e] = make_float2(pa[e], pz[e]);
-        }
-        warp_fft<N, 8, kFwd>(z, xs, t, ct);
-        float2 X[4], Y[4];
-        r2c_pair_unpack<N>(z, t, s2, X, Y);
-        if (fj == 0) {
-          if (valid) {
-            float2* dst = db + line * kt;
-            store_du_line<N>(dst, X, t, kt, kd);
-            store_du_line<N>(dst + ds, Y, t, kt, kd);
-          }
-        } else {
-          if (pvalid) store_du_line<N>(db + 2 * ds + line_of(2 * pair) * kt, X, t, kt, kd);
-          if (valid) store_du_line<N>(db + 2 * ds + line * kt, Y, t, kt, kd);
-        }
-        __syncwarp();
-      }
-      if (half == 0) {
+    for (int e = 0; e < 8; ++e) h2[e] = z[e];
+    __syncwarp();
+    c2r_pair_load<N>(src + 4 * fs, src + 5 * fs, t, z);  // curl_y + i curl_z
+    warp_fft<N, 8, kInv>(z, xs, t, ct);
+    __syncwarp();
+    // u x curl u at this lane's positions (unnormalised: the scale enters in s2)
 #pragma unroll
-        for (int e = 0; e < 8; ++e) pa[e] = pz[e];
-      }
+    for (int e = 0; e < 8; ++e) {
+      const float ux = h1[e].x, uy = h1[e].y, uz = h2[e].x, wx = h2[e].y, wy = z[e].x, wz = z[e].y;
+      const float pz = fmaf(ux, wy, -uy * wx);
+      if (half == 0)
+        pa[e] = pz;
+      else
+        pb[e] = pz;
+      z[e] = make_float2(fmaf(uy, wz, -uz * wy), fmaf(uz, wx, -ux * wz));
     }
-    base = nbase;
-    nbase = base < npairs ? grab() : npairs;
-  }
-  // the last CTA of this trajectory resets the counters for the next launch
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(ctr + 1, 1u) == gridDim.x - 1) {
-      atomicExch(ctr, 0u);
-      atomicExch(ctr + 1, 0u);
+    warp_fft<N, 8, kFwd>(z, xs, t, ct);
+    float2 X[4], Y[4];
+    r2c_pair_unpack<N>(z, t, s2, X, Y);
+    if (valid) {
+      float2* dst = db + line * kt;
+      store_du_line<N>(dst, X, t, kt, kd);
+      store_du_line<N>(dst + ds, Y, t, kt, kd);
     }
+    __syncwarp();
   }
+  // z components of lines A and B in one forward FFT
+  float2 z[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) z[e] = make_float2(pa[e], pb[e]);
+  warp_fft<N, 8, kFwd>(z, xs, t, ct);
+  float2 X[4], Y[4];
+  r2c_pair_unpack<N>(z, t, s2, X, Y);
+  if (ia < nlines) store_du_line<N>(db + 2 * ds + (nlines - 1 - ia) * kt, X, t, kt, kd);
+  if (ia + 1 < nlines) store_du_line<N>(db + 2 * ds + (nlines - 2 - ia) * kt, Y, t, kt, kd);
 }
 
 // ------------------------------------------------------------------------------

@@ -37,25 +37,34 @@ struct DnsOps {
     return 0;
   }
 
-  // resident CTAs (all SMs) of the persistent two-for-one line pass (0: one CTA per tile)
-  static inline int line2_ctas = 0;
-
   static void init_attrs() {
     if constexpr (N >= 64) {
       tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
       tma_plain_ctas = persistent_ctas(kx_inv_tma<N, false>);
     }
-    if constexpr (N >= 64 && N <= 256) {
-      int nb = 0, dev = 0, sms = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, line_cross2<N>, Line2Cfg<N>::THREADS, 0) ==
-              cudaSuccess &&
-          cudaGetDevice(&dev) == cudaSuccess &&
-          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-        line2_ctas = nb * sms;
-      else
-        cudaGetLastError();
-    }
+  }
+
+  // y pass of `nz` fields (columns [0, ncols) of rows of ncols values) in the plan's
+  // y schedule (KyCfg variant)
+  template <int DIR>
+  static void y_pass(const Ctx& c, int kind, double bytes, float2* w, long long fs, int ncols, int kd_store, int nz,
+                     cudaStream_t s) {
+    const dim3 g(ky_tiles(ncols), N, nz);
+    if (c.sched.y_var == 1)
+      L3ES_LAUNCH(c, kind, bytes, s,
+                  ky_pass<N, DIR, 1><<<g, KyCfg<N, 1>::THREADS, 0, s>>>(w, fs, ncols, ncols, kd_store, c.tw));
+    else
+      L3ES_LAUNCH(c, kind, bytes, s, ky_pass<N, DIR, 0><<<g, KY::THREADS, 0, s>>>(w, fs, ncols, ncols, kd_store, c.tw));
+  }
+
+  // the RHS's y inverse (six one-FFT jobs per tile) in the plan's y schedule
+  static void y_inv_rhs(const Ctx& c, double bytes, cudaStream_t s) {
+    const dim3 g(6 * ky_tiles(H), N, c.batch);
+    if (c.sched.y_var == 1)
+      L3ES_LAUNCH(c, KK_Y_INV, bytes, s, ky_inv_rhs<N, 1><<<g, KyCfg<N, 1>::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
+    else
+      L3ES_LAUNCH(c, KK_Y_INV, bytes, s, ky_inv_rhs<N, 0><<<g, KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
   }
 
   // x inverse pass with curl prologue: us -> W (6 fields)
@@ -67,7 +76,7 @@ struct DnsOps {
       const unsigned long long dims[3] = {(unsigned long long)mc, N, 3ull * c.batch};
       const unsigned long long strides[2] = {8ull * mc, 8ull * c.cs};
       const unsigned box[3] = {TW, KxTma<N>::NY, 3};
-      if (tma_ctas > 0 && tma_encode(&map, us, 3, dims, strides, box)) {
+      if (c.sched.x_bulk && tma_ctas > 0 && tma_encode(&map, us, 3, dims, strides, box)) {
         const int ntiles = (int)(mc / TW);
         const int gx = std::max(1, std::min(ntiles, tma_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_INV, bytes, s,
@@ -94,40 +103,39 @@ struct DnsOps {
     // 3D: the x pass stores u_x, curl_y, curl_z in W and u_y, u_z in the side buffer
     // Wx (curl_x is not stored); the y pass writes all six fields of W
     x_inverse<DIM>(c, us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
-    if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
-                  ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
+    if (DIM == 3) y_inv_rhs(c, 11.0 / 3.0 * A, s);
+    bool line_done = false;
     if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT, persistent
-      using L2 = Line2Cfg<N>;
-      const float s2 = 0.5f * scale * scale;
-      const long long tiles = (lines + L2::LPC - 1) / L2::LPC;
-      const long long cap = line2_ctas > 0 ? std::max(1, line2_ctas / c.batch) : tiles;
-      L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
-                  line_cross2<N><<<dim3((unsigned)std::min(tiles, cap), c.batch), L2::THREADS, 0, s>>>(
-                      c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines, c.work));
-    } else {
+      if (c.sched.line_pair) {
+        using L2 = Line2Cfg<N>;
+        const float s2 = 0.5f * scale * scale;
+        const long long tiles = (lines + L2::LPC - 1) / L2::LPC;
+        L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                    line_cross2<N><<<dim3((unsigned)tiles, c.batch), L2::THREADS, 0, s>>>(
+                        c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(), (int)lines));
+        line_done = true;
+      }
+    }
+    if (!line_done)
       L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
                   line_cross<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                       c.W, c.fs, c.DU, c.ds, c.kt, c.kd, scale, c.tw, (int)lines));
-    }
-    if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_FWD, Adu * (1.0 + rows), s,
-                  ky_pass<N, kFwd><<<dim3(ky_tiles(c.kt), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.DU, c.ds, c.kt, c.kt, c.kd,
-                                                                                  c.tw));
+    if (DIM == 3) y_pass<kFwd>(c, KK_Y_FWD, Adu * (1.0 + rows), c.DU, c.ds, c.kt, c.kd, 3 * c.batch, s);
     // band x-FFT + projection into P, then the elementwise RK update
     const int nb = 2 * c.kd + 1;
     const double Ap = 8.0 * 3.0 * c.pcs * B;
     // (block 0 of each trajectory also computes the constant-power coefficient of us)
     const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
     bool band_done = false;
-    // from 256^3: smaller grids have too few band tiles per persistent CTA to pipeline
-    // (measured at 128^3: 9.5 us persistent vs 8.4 us one-shot)
-    if constexpr (DIM == 3 && N >= 256) {
+    // by default from 256^3: smaller grids have too few band tiles per persistent CTA to
+    // pipeline (measured at 128^3: 9.5 us persistent vs 8.4 us one-shot)
+    if constexpr (DIM == 3 && N >= 64) {
+      const bool bulk = c.sched.band_bulk < 0 ? N >= 256 : c.sched.band_bulk != 0;
       CUtensorMap map;
       const unsigned long long dims[4] = {(unsigned long long)c.kt, N, N, 3ull * c.batch};
       const unsigned long long strides[3] = {8ull * c.kt, 8ull * N * c.kt, 8ull * c.ds};
       const unsigned box[4] = {TW, 1, KxTma<N>::NY, 3};
-      if (tma_band_ctas > 0 && tma_encode(&map, c.DU, 4, dims, strides, box)) {
+      if (bulk && tma_band_ctas > 0 && tma_encode(&map, c.DU, 4, dims, strides, box)) {
         const int ntiles = (c.kt / TW) * nb;
         const int gx = std::max(1, std::min(ntiles, tma_band_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
@@ -177,7 +185,7 @@ struct DnsOps {
       const unsigned long long dims[3] = {(unsigned long long)mc, N, 3ull * c.batch};
       const unsigned long long strides[2] = {8ull * mc, 8ull * c.cs};
       const unsigned box[3] = {TW, KxTma<N>::NY, 3};
-      if (tma_plain_ctas > 0 && tma_encode(&map, uh, 3, dims, strides, box)) {
+      if (c.sched.x_bulk && tma_plain_ctas > 0 && tma_encode(&map, uh, 3, dims, strides, box)) {
         const int ntiles = (int)(mc / TW);
         const int gx = std::max(1, std::min(ntiles, tma_plain_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
@@ -190,10 +198,7 @@ struct DnsOps {
       L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
                   kx_inv<N, DIM, false><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
                       uh, c.cs, c.W, c.fs, c.tw));
-    if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
-                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
-                                                                                         c.tw));
+    if (DIM == 3) y_pass<kInv>(c, KK_Y_INV, 2.0 * A, c.W, c.fs, H, N / 2, 3 * c.batch, s);
     L3ES_LAUNCH(c, KK_LINE_C2R, A + P, s,
                 line_c2r<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                     c.W, c.fs, u, c.ps, scale, c.tw, (int)lines));
@@ -214,10 +219,7 @@ struct DnsOps {
     L3ES_LAUNCH(c, KK_LINE_R2C, A + P, s,
                 line_r2c<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                     u, c.ps, c.W, c.fs, c.tw, (int)lines));
-    if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_FWD, 2.0 * A, s,
-                  ky_pass<N, kFwd><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(c.W, c.fs, H, H, N / 2,
-                                                                                         c.tw));
+    if (DIM == 3) y_pass<kFwd>(c, KK_Y_FWD, 2.0 * A, c.W, c.fs, H, N / 2, 3 * c.batch, s);
     L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 2.0 * A, s,
                 kx_fwd_plain<N, DIM><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
                     c.W, c.fs, uh, c.cs, c.tw));
@@ -248,19 +250,13 @@ struct DnsOps {
                     a.g, c.cs, a.gscale, c.kd, Wm, c.fs, c.tw, a.us, a.band_kf2 > 0 ? c.kf : 0, inv_n2d,
                     c.eps_inj, const_cast<double*>(a.band_adj)));
     if (DIM == 3) {
-      L3ES_LAUNCH(c, KK_Y_INV, 11.0 / 3.0 * A, s,
-                  ky_inv_rhs<N><<<dim3(6 * ky_tiles(H), N, c.batch), KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
-      L3ES_LAUNCH(c, KK_Y_INV, 2.0 * A, s,
-                  ky_pass<N, kInv><<<dim3(ky_tiles(H), N, 3 * c.batch), KY::THREADS, 0, s>>>(Wm, c.fs, H, H, N / 2,
-                                                                                         c.tw));
+      y_inv_rhs(c, 11.0 / 3.0 * A, s);
+      y_pass<kInv>(c, KK_Y_INV, 2.0 * A, Wm, c.fs, H, N / 2, 3 * c.batch, s);
     }
     L3ES_LAUNCH(c, KK_ADJ_LINE, 5.0 * A, s,
                 line_cross_adj<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
                     Wm, c.W, c.fs, Y6, c.cs, scale, c.tw, (int)lines));
-    if (DIM == 3)
-      L3ES_LAUNCH(c, KK_Y_FWD, 4.0 * A, s,
-                  ky_pass<N, kFwd><<<dim3(ky_tiles(H), N, 6 * c.batch), KY::THREADS, 0, s>>>(Y6, c.cs, H, H, N / 2,
-                                                                                         c.tw));
+    if (DIM == 3) y_pass<kFwd>(c, KK_Y_FWD, 4.0 * A, Y6, c.cs, H, N / 2, 6 * c.batch, s);
     // Y6 (6 fields per trajectory) -> W, as 2 * batch groups of 3 fields
     L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 4.0 * A, s,
                 kx_fwd_plain<N, DIM><<<dim3(xb, 2 * c.batch), TX, 0, s>>>(Y6, c.cs, c.W, c.fs, c.tw));

@@ -118,6 +118,15 @@ bool tma_encode(CUtensorMap* map, const void* base, int rank, const unsigned lon
 // caller arrays must start on a 16-byte boundary (checked at the C entry points).
 inline bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) != 0; }
 
+// Kernel variants of one plan's step (chosen by l3es_plan_autotune; the defaults are the
+// measured best at 256^3 on GB300).
+struct Schedule {
+  int x_bulk = 1;     // 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA)
+  int y_var = 0;      // y-pass schedule: KyCfg variant (0: radix 16 from N = 128, 1: radix 8)
+  int line_pair = 1;  // two-for-one line pass for 64 <= N <= 256 (else the packed half-length pass)
+  int band_bulk = -1; // persistent bulk-copy band pass (-1: from N = 256, the measured default)
+};
+
 // Geometry + scratch of one plan, handed to the per-N launch wrappers.
 struct Ctx {
   int dim = 3, n = 0, h = 0, batch = 1;
@@ -145,7 +154,7 @@ struct Ctx {
   double* einj = nullptr;      // [batch] scratch e_inj
   float* nu_b = nullptr;       // [batch] viscosity per trajectory
   int* err = nullptr;          // device error word: nonzero after a kernel wait timed out
-  unsigned* work = nullptr;    // [batch][2] work counters of the persistent line pass (zero between launches)
+  Schedule sched;              // kernel variants of the step
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate
   KTimer* timer = nullptr;     // per-launch timing (nullptr = off)

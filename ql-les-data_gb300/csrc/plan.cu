@@ -264,7 +264,6 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   rc = rc ? rc : plan_alloc(p, (void**)&c.einj, sizeof(double) * B, "einj");
   rc = rc ? rc : plan_alloc(p, (void**)&c.nu_b, sizeof(float) * B, "viscosities");
   rc = rc ? rc : plan_alloc(p, (void**)&c.err, sizeof(int), "error word");
-  rc = rc ? rc : plan_alloc(p, (void**)&c.work, sizeof(unsigned) * 2 * B, "work counters");
   if (rc != L3ES_OK) {
     plan_free(p);
     delete p;
@@ -277,7 +276,6 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   if (e == cudaSuccess) e = cudaMemcpy(c.e0, e0.data(), sizeof(double) * B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c.band, 0, sizeof(double) * B);
   if (e == cudaSuccess) e = cudaMemset(c.err, 0, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(c.work, 0, sizeof(unsigned) * 2 * B);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     rc = cuda_check(e, "l3es_plan_create");
@@ -391,7 +389,154 @@ int32_t l3es_kernel_kind_count(void) { return KK_COUNT; }
 
 const char* l3es_kernel_kind_name(int32_t kind) { return kernel_kind_name(kind); }
 
+int l3es_plan_get_schedule(const l3es_plan* plan, int32_t* sched4) {
+  if (!plan || !sched4) return fail(L3ES_EINVAL, "l3es_plan_get_schedule: null argument");
+  const Schedule& s = plan->ctx.sched;
+  sched4[0] = s.x_bulk;
+  sched4[1] = s.y_var;
+  sched4[2] = s.line_pair;
+  sched4[3] = s.band_bulk < 0 ? (plan->ctx.n >= 256 ? 1 : 0) : s.band_bulk;
+  return L3ES_OK;
+}
+
+int l3es_plan_set_schedule(l3es_plan* plan, const int32_t* sched4) {
+  if (!plan || !sched4) return fail(L3ES_EINVAL, "l3es_plan_set_schedule: null argument");
+  for (int i = 0; i < 4; ++i)
+    if (sched4[i] != 0 && sched4[i] != 1) return fail(L3ES_EINVAL, "l3es_plan_set_schedule: values are 0 or 1");
+  Schedule& s = plan->ctx.sched;
+  s.x_bulk = sched4[0];
+  s.y_var = sched4[1];
+  s.line_pair = sched4[2];
+  s.band_bulk = sched4[3];
+  return L3ES_OK;
+}
+
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Autotuner: picks the plan's kernel variants (bulk-copy or one-tile x passes, radix-16 or
+// radix-8 y passes, two-for-one or packed line pass, bulk-copy or one-tile band pass) by
+// timing the right-hand side on the plan's own scratch (coordinate descent, each knob
+// with the others at their current choice), and caches the result in a text file, one
+// line per (GPU, dim, N, batch): "<key> x_bulk y_var line_pair band_bulk".
+// ---------------------------------------------------------------------------------
+static std::string tune_key(const l3es_plan* p) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, p->device);
+  std::string name = prop.name;
+  for (char& ch : name)
+    if (ch == ' ') ch = '_';
+  return name + "|sm" + std::to_string(prop.major) + std::to_string(prop.minor) + "|d" + std::to_string(p->ctx.dim) +
+         "|n" + std::to_string(p->ctx.n) + "|b" + std::to_string(p->ctx.batch);
+}
+
+static bool tune_cache_read(const char* path, const std::string& key, int32_t* v) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof line, f)) {
+    char k[400];
+    int a, b, c, d;
+    if (std::sscanf(line, "%399s %d %d %d %d", k, &a, &b, &c, &d) == 5 && key == k) {
+      v[0] = a;
+      v[1] = b;
+      v[2] = c;
+      v[3] = d;
+      found = true;  // the last entry of a key wins
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+static void tune_cache_write(const char* path, const std::string& key, const int32_t* v) {
+  if (!path) return;
+  std::vector<std::string> keep;
+  if (FILE* f = std::fopen(path, "r")) {
+    char line[512];
+    while (std::fgets(line, sizeof line, f)) {
+      char k[400];
+      if (std::sscanf(line, "%399s", k) == 1 && key == k) continue;
+      keep.emplace_back(line);
+    }
+    std::fclose(f);
+  }
+  FILE* f = std::fopen(path, "w");
+  if (!f) return;  // an unwritable cache only costs a re-tune
+  for (const auto& l : keep) std::fputs(l.c_str(), f);
+  std::fprintf(f, "%s %d %d %d %d\n", key.c_str(), v[0], v[1], v[2], v[3]);
+  std::fclose(f);
+}
+
+// mean milliseconds of one right-hand side with the plan's current schedule
+static float time_rhs(l3es_plan* p, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+  const Ctx& c = p->ctx;
+  const l3es_plan_desc& d = p->desc;
+  EpiParams prm{};
+  prm.nu = (float)d.nu;
+  prm.drag = (float)d.drag;
+  prm.kolm_amp = (float)d.kolm_amp;
+  prm.kolm_k = d.kolm_k;
+  prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
+  prm.rk = -1;
+  for (int i = 0; i < 2; ++i) p->tab.stage(c, c.Tb, nullptr, c.C, -1, prm, s);
+  const int reps = c.cs * c.batch > (1 << 20) ? 5 : 20;
+  cudaEventRecord(e0, s);
+  for (int i = 0; i < reps; ++i) p->tab.stage(c, c.Tb, nullptr, c.C, -1, prm, s);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  return ms / reps;
+}
+
+extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void* stream) {
+  if (!plan) return fail(L3ES_EINVAL, "l3es_plan_autotune: null plan");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  int rc = cuda_check(cudaStreamIsCapturing(s, &cap), "l3es_plan_autotune");
+  if (rc != L3ES_OK) return rc;
+  if (cap != cudaStreamCaptureStatusNone) return fail(L3ES_ESTATE, "l3es_plan_autotune: not while recording a graph");
+  const std::string key = tune_key(plan);
+  int32_t v[4];
+  if (tune_cache_read(cache_path, key, v)) return l3es_plan_set_schedule(plan, v);
+  Ctx& c = plan->ctx;
+  KTimer* timer = c.timer;
+  c.timer = nullptr;  // untimed by the per-kernel timer
+  rc = cuda_check(cudaMemsetAsync(c.Tb, 0, sizeof(float2) * 3 * c.cs * c.batch, s), "l3es_plan_autotune memset");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == L3ES_OK) rc = cuda_check(cudaEventCreate(&e0), "l3es_plan_autotune event");
+  if (rc == L3ES_OK) rc = cuda_check(cudaEventCreate(&e1), "l3es_plan_autotune event");
+  if (rc == L3ES_OK) {
+    l3es_plan_get_schedule(plan, v);
+    l3es_plan_set_schedule(plan, v);
+    // knobs that change anything for this plan
+    const int n = c.n;
+    const bool knob[4] = {c.dim == 3 && n >= 64, c.dim == 3 && n >= 128, n >= 64 && n <= 256,
+                          c.dim == 3 && n >= 64};
+    float best = time_rhs(plan, s, e0, e1);
+    for (int k = 0; k < 4; ++k) {
+      if (!knob[k]) continue;
+      v[k] ^= 1;
+      l3es_plan_set_schedule(plan, v);
+      const float t = time_rhs(plan, s, e0, e1);
+      if (t < best) {
+        best = t;
+      } else {
+        v[k] ^= 1;
+        l3es_plan_set_schedule(plan, v);
+      }
+    }
+    rc = cuda_check(cudaGetLastError(), "l3es_plan_autotune launch");
+    if (rc == L3ES_OK) tune_cache_write(cache_path, key, v);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  c.timer = timer;
+  return rc;
+}
 
 // per-block partial sums of w |u_hat|^2 into c.partial ([batch][nblk]); returns nblk
 int l3es::energy_partials(const Ctx& c, const float2* uh, cudaStream_t s) {

@@ -28,6 +28,9 @@ _SIGNATURES = {
     "l3es_plan_set_e0": (ctypes.c_int, [_P, _P, _I]),
     "l3es_plan_workspace_bytes": (ctypes.c_int64, [_P]),
     "l3es_plan_set_nu": (ctypes.c_int, [_P, _P, _I]),
+    "l3es_plan_get_schedule": (ctypes.c_int, [_P, _P]),
+    "l3es_plan_set_schedule": (ctypes.c_int, [_P, _P]),
+    "l3es_plan_autotune": (ctypes.c_int, [_P, ctypes.c_char_p, _P]),
     "l3es_graph_begin": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "l3es_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "l3es_graph_launch": (ctypes.c_int, [_P, _P]),
@@ -310,6 +313,34 @@ class Plan:
     @property
     def workspace_bytes(self) -> int:
         return int(self._lib.l3es_plan_workspace_bytes(self._h))
+
+    SCHEDULE_KEYS = ("x_bulk", "y_radix8", "line_pair", "band_bulk")
+
+    @property
+    def schedule(self) -> dict:
+        """The plan's kernel schedule (l3es_plan_get_schedule) as {name: 0 or 1}."""
+        v = (ctypes.c_int32 * 4)()
+        _check(self._lib.l3es_plan_get_schedule(self._h, v), "l3es_plan_get_schedule")
+        return dict(zip(self.SCHEDULE_KEYS, list(v)))
+
+    def set_schedule(self, sched: dict) -> None:
+        cur = self.schedule
+        cur.update(sched)
+        v = (ctypes.c_int32 * 4)(*[int(cur[k]) for k in self.SCHEDULE_KEYS])
+        _check(self._lib.l3es_plan_set_schedule(self._h, v), "l3es_plan_set_schedule")
+
+    def autotune(self, cache_path=None, stream=None) -> dict:
+        """Pick the fastest kernel schedule for this plan (l3es_plan_autotune); cache_path
+        defaults to $L3ES_TUNE_CACHE or ~/.cache/l3es_gb300/schedules.txt ("" = no
+        cache). Returns the chosen schedule."""
+        if cache_path is None:
+            cache_path = os.environ.get("L3ES_TUNE_CACHE",
+                                        os.path.join(os.path.expanduser("~"), ".cache", "l3es_gb300", "schedules.txt"))
+        if cache_path:
+            os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)
+        path = cache_path.encode() if cache_path else None
+        _check(self._lib.l3es_plan_autotune(self._h, path, _stream(stream)), "l3es_plan_autotune")
+        return self.schedule
 
     def close(self) -> None:
         if getattr(self, "_h", None):

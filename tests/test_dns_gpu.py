@@ -415,3 +415,39 @@ def test_integrating_factor_decays_a_shear_mode_exactly():
     out = torch.empty(p.phys_shape, dtype=torch.float32, device="cuda")
     p.irfftn(g, out)
     assert np.abs(out.cpu().numpy() - np.exp(-nu * dt * steps) * u).max() < 1e-6
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_every_kernel_schedule_gives_the_same_step(n):
+    """The 16 kernel schedules (x pass, y-pass radix, line pass, band pass variants)
+    compute the same RK4 step to FP32 rounding (against the default schedule)."""
+    import itertools
+
+    u0 = R.init_u_hit(n, 3, spectrum="k4exp", kp=3.0)
+    uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
+    p = _plan(dim=3, n=n, nu=5e-3, dt=2e-3, forcing="const_power", kf=2, eps_inj=0.1)
+    ref = _c64(uh0)
+    p.step(ref, 2)
+    ref = ref.cpu().numpy()
+    keys = p.SCHEDULE_KEYS
+    for combo in itertools.product((0, 1), repeat=4):
+        p.set_schedule(dict(zip(keys, combo)))
+        g = _c64(uh0)
+        p.step(g, 2)
+        p.check()
+        assert _rel(g.cpu().numpy(), ref) < 2e-6, combo
+
+
+def test_autotune_picks_a_schedule_and_caches_it(tmp_path):
+    from l3es import _native
+
+    cache = str(tmp_path / "sched.txt")
+    p = _plan(dim=3, n=128, nu=5e-3, dt=2e-3)
+    s1 = p.autotune(cache)
+    assert set(s1) == set(_native.Plan.SCHEDULE_KEYS) and all(v in (0, 1) for v in s1.values())
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1 and "|d3|n128|b1" in lines[0]
+    q = _plan(dim=3, n=128, nu=1e-2, dt=1e-3)
+    q.set_schedule({k: 1 - v for k, v in s1.items()})
+    assert q.autotune(cache) == s1  # read from the cache, not re-timed
+    assert len(open(cache).read().splitlines()) == 1
