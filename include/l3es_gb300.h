@@ -101,10 +101,12 @@ int l3es_plan_set_nu(l3es_plan* plan, const double* nu_host, int32_t count);
 int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
 
 /* Kernel schedule of the plan's step (no counterpart in the reference, whose XLA
- * compiler picks its own kernels, spectral_solver.py:130-153): four 0/1 choices,
+ * compiler picks its own kernels, spectral_solver.py:130-153): four choices,
  *   [0] 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA),
  *   [1] y passes with the radix-8 schedule (else radix 16 from N = 128),
- *   [2] the two-for-one half-axis line pass for 64 <= N <= 256 (else the packed one),
+ *   [2] the half-axis line pass: 1 two-for-one for 64 <= N <= 256, 2 two-for-one with
+ *       radix-16 line FFTs, 3 the same fed by bulk copies (2 and 3: N = 256 only),
+ *       0 the packed half-length one,
  *   [3] the persistent bulk-copy band x pass (else one tile per CTA).
  * Every schedule computes the same step; only speed differs. */
 int l3es_plan_get_schedule(const l3es_plan* plan, int32_t* sched4);

@@ -37,7 +37,14 @@ struct DnsOps {
     return 0;
   }
 
+  static inline bool lc3_staged_ok = false;  // dynamic shared memory of the staged line pass granted
+
   static void init_attrs() {
+    if constexpr (N == 256) {
+      lc3_staged_ok = cudaFuncSetAttribute(line_cross3<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           Line3Cfg<N>::SMEM_STAGED) == cudaSuccess;
+      cudaGetLastError();
+    }
     if constexpr (N >= 64) {
       tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
@@ -106,7 +113,25 @@ struct DnsOps {
     if (DIM == 3) y_inv_rhs(c, 11.0 / 3.0 * A, s);
     bool line_done = false;
     if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT, persistent
-      if (c.sched.line_pair) {
+      if constexpr (N == 256) {
+        if (c.sched.line_pair >= 2) {  // radix-16 lines, 16 lanes per line
+          using L3 = Line3Cfg<N>;
+          const float s2 = 0.5f * scale * scale;
+          const long long tiles = (lines + L3::LPC - 1) / L3::LPC;
+          if (c.sched.line_pair == 3 && lc3_staged_ok && lines % L3::LPC == 0)
+            L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                        line_cross3<N, true><<<dim3((unsigned)tiles, c.batch), L3::THREADS, L3::SMEM_STAGED, s>>>(
+                            c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(),
+                            c.tw + line3_ct16_offset<N>(), (int)lines, c.err));
+          else
+            L3ES_LAUNCH(c, KK_LINE_CROSS, 2.0 * A + Adu, s,
+                        line_cross3<N, false><<<dim3((unsigned)tiles, c.batch), L3::THREADS, 0, s>>>(
+                            c.W, c.fs, c.DU, c.ds, c.kt, c.kd, s2, c.tw + line2_ct_offset<N>(),
+                            c.tw + line3_ct16_offset<N>(), (int)lines, c.err));
+          line_done = true;
+        }
+      }
+      if (!line_done && c.sched.line_pair) {
         using L2 = Line2Cfg<N>;
         const float s2 = 0.5f * scale * scale;
         const long long tiles = (lines + L2::LPC - 1) / L2::LPC;
@@ -152,10 +177,18 @@ struct DnsOps {
                       c.eps_inj, c.band));
     // rk -1: us -> du; 0: us -> out; 1: us, u0 -> acc, out; 2: us, u0, acc -> acc, out;
     // 3: us, acc -> fin
-    const double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);
+    double upd = Ap + A * (rk < 0 ? 2.0 : rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);
+    if (prm.lin && rk >= 0 && !(prm.if_h > 0.f)) {  // outside the stage region: u0 in, one field out
+      const double fr = DIM == 3 ? (2.0 * c.kd + 1.0) / N : (double)c.kt / H;
+      upd = Ap + A * (fr * (rk == 0 ? 2.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0) + (1.0 - fr) * 2.0);
+    }
     const long long pairs = 3 * c.cs / 2;
     const dim3 ug((unsigned)((pairs + 255) / 256), c.batch);
-    if (prm.if_h > 0.f && rk >= 0)
+    if (prm.lin && rk >= 0 && !(prm.if_h > 0.f))
+      L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
+                  k_rk_update_lin<N, DIM><<<ug, 256, 0, s>>>(c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm,
+                                                            c.band, c.nu_b, c.err));
+    else if (prm.if_h > 0.f && rk >= 0)
       L3ES_LAUNCH(c, KK_RK_UPDATE, upd, s,
                   k_rk_update<N, DIM, true><<<ug, 256, 0, s>>>(c.P, c.pcs, c.kt, c.kd, us, S, c.C, out, S, c.cs, prm,
                                                                 c.band, c.nu_b, c.err));

@@ -123,7 +123,8 @@ inline bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p)
 struct Schedule {
   int x_bulk = 1;     // 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA)
   int y_var = 0;      // y-pass schedule: KyCfg variant (0: radix 16 from N = 128, 1: radix 8)
-  int line_pair = 1;  // two-for-one line pass for 64 <= N <= 256 (else the packed half-length pass)
+  int line_pair = 1;  // line pass: 1 two-for-one (64 <= N <= 256), 2 two-for-one radix 16 and 3 the same
+                      // fed by bulk copies (N = 256; 3 is its default), 0 packed
   int band_bulk = -1; // persistent bulk-copy band pass (-1: from N = 256, the measured default)
 };
 
@@ -154,6 +155,7 @@ struct Ctx {
   double* einj = nullptr;      // [batch] scratch e_inj
   float* nu_b = nullptr;       // [batch] viscosity per trajectory
   int* err = nullptr;          // device error word: nonzero after a kernel wait timed out
+  int lin_enabled = 1;         // closed-form RK stages outside the stage region (run_steps)
   Schedule sched;              // kernel variants of the step
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate

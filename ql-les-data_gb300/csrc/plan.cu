@@ -98,12 +98,12 @@ static float2 twiddle(long long m, long long n) {
   return make_float2((float)std::cos(a), (float)std::sin(a));
 }
 
-// Appends the compact per-stage table of an m-point FFT (radix-8 schedule; Sched::ctoff
-// layout): for stage s >= 1 of radix R with Ns points per sub-transform, entries
+// Appends the compact per-stage table of an m-point FFT (stages of radix radix_max until
+// the remainder is smaller; Sched::ctoff layout): for stage s >= 1 of radix R with Ns points per sub-transform, entries
 // r = 1..R-1, jm = 0..Ns-1 hold exp(-2 pi i r jm / (Ns R)). Same FP64 angles (scaled by
 // powers of two) as the strided table, so both give the same FP32 values.
-static void push_compact_table(std::vector<float2>& t, int m) {
-  const int E = m >= 8 ? 8 : m;
+static void push_compact_table(std::vector<float2>& t, int m, int radix_max = 8) {
+  const int E = m >= radix_max ? radix_max : m;
   std::vector<int> radix;
   int rem = m;
   while (E > 1 && rem >= E) {
@@ -122,13 +122,15 @@ static void push_compact_table(std::vector<float2>& t, int m) {
 }
 
 // FP64 -> FP32 twiddle table exp(-2 pi i m / n), m in [0, n), followed by the compact
-// table of the n/2-point line FFT and that of the n-point FFT (the two-for-one line
-// pass, at line2_ct_offset<n>()).
+// table of the n/2-point line FFT, that of the n-point FFT (the two-for-one line pass,
+// at line2_ct_offset<n>()) and that of the n-point FFT in radix-16 stages (at
+// line3_ct16_offset<n>()).
 static std::vector<float2> twiddles(int n) {
   std::vector<float2> t(n);
   for (int m = 0; m < n; ++m) t[m] = twiddle(m, n);
   push_compact_table(t, n / 2);
   push_compact_table(t, n);
+  push_compact_table(t, n, 16);  // radix-16 line pass (line3_ct16_offset<n>())
   return t;
 }
 
@@ -234,6 +236,7 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   c.batch = desc->batch;
   c.kd = dealias_kd(n);
   c.kt = ((c.kd + 1 + TW - 1) / TW) * TW;
+  if (n == 256) c.sched.line_pair = 3;  // the staged radix-16 line pass (measured best at 256)
   c.nmid = dim == 3 ? n : 1;
   c.cs = c.nmid * n * c.h;
   c.fs = c.cs;
@@ -402,7 +405,10 @@ int l3es_plan_get_schedule(const l3es_plan* plan, int32_t* sched4) {
 int l3es_plan_set_schedule(l3es_plan* plan, const int32_t* sched4) {
   if (!plan || !sched4) return fail(L3ES_EINVAL, "l3es_plan_set_schedule: null argument");
   for (int i = 0; i < 4; ++i)
-    if (sched4[i] != 0 && sched4[i] != 1) return fail(L3ES_EINVAL, "l3es_plan_set_schedule: values are 0 or 1");
+    if (sched4[i] != 0 && sched4[i] != 1 && !(i == 2 && (sched4[i] == 2 || sched4[i] == 3)))
+      return fail(L3ES_EINVAL, "l3es_plan_set_schedule: values are 0 or 1 (line pass: 0 to 3)");
+  if (sched4[2] >= 2 && plan->ctx.n != 256)
+    return fail(L3ES_EINVAL, "l3es_plan_set_schedule: the radix-16 line passes (2, 3) exist for N = 256 only");
   Schedule& s = plan->ctx.sched;
   s.x_bulk = sched4[0];
   s.y_var = sched4[1];
@@ -516,18 +522,24 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
     const int n = c.n;
     const bool knob[4] = {c.dim == 3 && n >= 64, c.dim == 3 && n >= 128, n >= 64 && n <= 256,
                           c.dim == 3 && n >= 64};
+    const int nval[4] = {2, 2, n == 256 ? 4 : 2, 2};  // the line pass has two radix-16 forms at 256
     float best = time_rhs(plan, s, e0, e1);
     for (int k = 0; k < 4; ++k) {
       if (!knob[k]) continue;
-      v[k] ^= 1;
-      l3es_plan_set_schedule(plan, v);
-      const float t = time_rhs(plan, s, e0, e1);
-      if (t < best) {
-        best = t;
-      } else {
-        v[k] ^= 1;
+      const int keep = v[k];
+      int pick = keep;
+      for (int val = 0; val < nval[k]; ++val) {
+        if (val == keep) continue;
+        v[k] = val;
         l3es_plan_set_schedule(plan, v);
+        const float t = time_rhs(plan, s, e0, e1);
+        if (t < best) {
+          best = t;
+          pick = val;
+        }
       }
+      v[k] = pick;
+      l3es_plan_set_schedule(plan, v);
     }
     rc = cuda_check(cudaGetLastError(), "l3es_plan_autotune launch");
     if (rc == L3ES_OK) tune_cache_write(cache_path, key, v);
@@ -562,6 +574,11 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
   static const double b_rk4[3] = {0.5, 0.5, 1.0};
   const double inv_n2d = 1.0 / std::pow((double)c.n, 2 * c.dim);
   const double eps64 = 2.220446049250313e-16;  // jnp.finfo(float).eps, spectral_solver.py:23
+  // closed-form stages outside the stage region (k_rk_update): explicit scheme, forcing
+  // terms inside the region (band forcing |k| <= kf, Kolmogorov mode kh = kolm_k)
+  const int kf_band = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf : 0;
+  const int lin_ok = c.lin_enabled && d.scheme != L3ES_SCHEME_INTEGRATING_FACTOR && kf_band <= c.kd &&
+                     kf_band < c.kt && (d.kolm_k <= 0 || d.kolm_k < c.kt);
   for (int st = 0; st < nsteps; ++st) {
     for (int rk = 0; rk < 4; ++rk) {
       EpiParams prm;
@@ -574,6 +591,8 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
       prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
       prm.rk = rk;
       prm.if_h = d.scheme == L3ES_SCHEME_INTEGRATING_FACTOR ? (float)d.dt : 0.f;
+      prm.dt = (float)d.dt;
+      prm.lin = lin_ok;
       plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
     }
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;

@@ -57,6 +57,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
   return false;
 }
 
+// 1D bulk copy global -> shared of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned), completion counted in bytes on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  unsigned long long g;
+  asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(reinterpret_cast<unsigned long long>(src)));
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(g), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
 // 3D tiled bulk tensor load global -> shared, completion counted in bytes on `bar`.
 // The innermost coordinate x must keep x * element size a multiple of 16 bytes.
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {

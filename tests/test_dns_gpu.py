@@ -176,6 +176,34 @@ def test_rhs_outside_dealias_band_is_viscous_only(dim, n):
     assert _rel(d, ref) < RTOL
 
 
+@pytest.mark.parametrize("k", [(1, 2, 3), (1, 1, 26), (2, 30, 1), (3, -25, 28), (-5, 0, 23)])
+def test_single_mode_decays_by_the_rk4_polynomial(k):
+    """One transverse Fourier mode has u x curl u parallel to k (a gradient the projection
+    removes), so each RK4 step multiplies it by R(-z) = 1 - z + z^2/2 - z^3/6 + z^4/24,
+    z = nu |k|^2 dt. At 64^3 (kd = 21, kt = 24) the cases lie in the dealiasing cube,
+    outside it along kz (kz = 23, 26, 28: still in the rows the RK update treats in full)
+    and outside the rows |ky| <= kd, where the update takes the closed form; the step
+    must give the same factor on every path. Outside the dealiasing cube the mode's 2k product aliases onto
+    another wavenumber, so the amplitude is kept at 1e-9: that quadratic residue stays
+    below FP32 rounding of the mode itself."""
+    n, nu, dt, steps = 64, 5e-4, 0.4, 5
+    kx, ky, kz = k
+    kvec = np.array([kx, ky, kz], dtype=np.float64)
+    a = np.cross(kvec, [0.3, -0.7, 0.5]) + 1j * np.cross(kvec, [0.2, 0.4, -0.1])  # a . k = 0
+    a *= 1e-9 / np.abs(a).max()
+    uh0 = np.zeros((3, n, n, n // 2 + 1), dtype=np.complex128)
+    uh0[:, kx % n, ky % n, kz] = a * n**3
+    z = nu * float(kvec @ kvec) * dt
+    rz = 1 - z + z**2 / 2 - z**3 / 6 + z**4 / 24
+    p = _plan(dim=3, n=n, nu=nu, dt=dt)
+    g = _c64(uh0)
+    p.step(g, steps)
+    p.check()
+    got = g.cpu().numpy()
+    want = uh0 * rz**steps
+    assert _rel(got, want) < 2e-6, (k, z)
+
+
 def test_step3d_512_vs_fp64():
     """The largest compiled grid, 512^3: two RK4 steps with constant-power forcing
     against the FP64 torch restatement of the same step (tests/_fp64_torch.py, equal
@@ -419,8 +447,9 @@ def test_integrating_factor_decays_a_shear_mode_exactly():
 
 @pytest.mark.parametrize("n", [64, 128, 256])
 def test_every_kernel_schedule_gives_the_same_step(n):
-    """The 16 kernel schedules (x pass, y-pass radix, line pass, band pass variants)
-    compute the same RK4 step to FP32 rounding (against the default schedule)."""
+    """The kernel schedules (x pass, y-pass radix, line pass, band pass variants; at 256
+    also the radix-16 line passes) compute the same RK4 step to FP32 rounding
+    (against the default schedule)."""
     import itertools
 
     u0 = R.init_u_hit(n, 3, spectrum="k4exp", kp=3.0)
@@ -430,12 +459,37 @@ def test_every_kernel_schedule_gives_the_same_step(n):
     p.step(ref, 2)
     ref = ref.cpu().numpy()
     keys = p.SCHEDULE_KEYS
-    for combo in itertools.product((0, 1), repeat=4):
+    line_vals = (0, 1, 2, 3) if n == 256 else (0, 1)
+    for combo in itertools.product((0, 1), (0, 1), line_vals, (0, 1)):
         p.set_schedule(dict(zip(keys, combo)))
         g = _c64(uh0)
         p.step(g, 2)
         p.check()
         assert _rel(g.cpu().numpy(), ref) < 2e-6, combo
+
+
+def test_line_pass_variants_agree_in_2d_at_256():
+    """2D Kolmogorov flow at 256^2 (drag, sin 4y forcing): every line pass variant gives
+    the same steps, and the radix-16 forms against the FP64 oracle."""
+    n, nu, dt, steps = 256, 1e-3, 1e-3, 3
+    u = R.init_u_random2d(n, 11)  # |k| <= 8, KE 0.5
+    uh0 = np.fft.rfftn(u, axes=(1, 2)).squeeze()
+    p = _plan(dim=2, n=n, nu=nu, dt=dt, drag=0.1, kolm_k=4, kolm_amp=1.0)
+    outs = {}
+    for lp in (0, 1, 2, 3):
+        p.set_schedule({"line_pair": lp})
+        g = _c64(uh0)
+        p.step(g, steps)
+        p.check()
+        outs[lp] = g.cpu().numpy()
+    for lp in (0, 2, 3):
+        assert _rel(outs[lp], outs[1]) < 2e-6, lp
+    rhs = R.rhs_wrapper(n, nu, (1, 2), drag=0.1, force_hat=R.kolmogorov_forcing_hat(n, 1.0, 4))
+    step = R.rk4_wrapper(dt, rhs, None, 0.0, "none", (1, 2))
+    uu, uh = u, uh0
+    for _ in range(steps):
+        uu, uh, _ = step(uu, uh)
+    assert _rel(outs[2], uh) < 2e-5 and _rel(outs[3], uh) < 2e-5
 
 
 def test_autotune_picks_a_schedule_and_caches_it(tmp_path):
