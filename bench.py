@@ -49,7 +49,8 @@ TRAFFIC_KERNELS = {"line_cross": ("line_cross<256", "line_cross2<256", "line_cro
                    "ky_pass_inv": ("ky_inv_rhs<256",),
                    "kx_inv_curl": ("kx_inv_tma<256, 1, 1>", "kx_inv_tma<256, true, true>",
                                    "kx_inv<256, 3, 1, 1>", "kx_inv<256, 3, true, true>"),
-                   "rk_update": ("k_rk_update<256",), "kx_fwd_band": ("kx_fwd_band<256", "kx_fwd_band_tma<256"),
+                   "rk_update": ("k_rk_update<256", "k_rk_update_lin<256"),
+                   "kx_fwd_band": ("kx_fwd_band<256", "kx_fwd_band_tma<256"),
                    "ky_pass_fwd": ("ky_pass<256, (int)-1", "ky_pass<256, -1")}
 
 
