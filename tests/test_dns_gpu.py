@@ -233,6 +233,46 @@ def test_step3d_512_vs_fp64():
     assert abs(float(ke) - ke64) < 1e-6 * ke64
 
 
+def test_step3d_256_fifty_steps_vs_fp64():
+    """The headline workload's step at full size (256^3, Rogallo k^4 exp init at KE 0.5,
+    constant-power forcing eps = 0.1 on |k| <= 2, nu = 5e-3, dt = 4.87e-3, every kernel
+    the bench times) over 50 steps against the FP64 torch restatement: the whole field,
+    the kinetic energy and the shell spectrum."""
+    from _fp64_torch import Fp64Model
+
+    n, nu, dt, steps = 256, 5e-3, 4.87e-3, 50
+    u0 = R.init_u_hit(n, 0, spectrum="k4exp", kp=4.0)
+    u0 *= np.sqrt(0.5 / R.kinetic_energy(u0))
+    uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
+    del u0
+    M = Fp64Model(n, nu, dt, kf=2, eps_inj=0.1)
+    ref = torch.from_numpy(uh0).cuda()
+    for _ in range(steps):
+        ref = M.step(ref)
+    p = _plan(dim=3, n=n, nu=nu, dt=dt, forcing="const_power", kf=2, eps_inj=0.1)
+    uh = _c64(uh0)
+    del uh0
+    p.step(uh, steps)
+    p.check()
+    d = uh.to(torch.complex128) - ref
+    assert float(d.abs().max() / ref.abs().max()) < RTOL
+    assert float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref)) < 1e-5
+    w = M.w
+    e32 = (w * (uh.to(torch.complex128).abs() ** 2).sum(0)).sum()
+    e64 = (w * (ref.abs() ** 2).sum(0)).sum()
+    assert abs(float(e32 / e64) - 1.0) < 1e-6
+    # shell spectrum, shells 1..85 (the dealiased range)
+    kx = torch.fft.fftfreq(n, 1.0 / n, dtype=torch.float64, device="cuda")
+    kz = torch.arange(n // 2 + 1, dtype=torch.float64, device="cuda")
+    kk = torch.sqrt(kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2)
+    shell = (kk + 0.5).long().clamp(max=n)
+    e_a = torch.zeros(n + 1, dtype=torch.float64, device="cuda").index_add_(
+        0, shell.flatten(), (w * (uh.to(torch.complex128).abs() ** 2).sum(0)).flatten())
+    e_b = torch.zeros(n + 1, dtype=torch.float64, device="cuda").index_add_(
+        0, shell.flatten(), (w * (ref.abs() ** 2).sum(0)).flatten())
+    assert float(((e_a - e_b).abs() / e_b)[1:86].max()) < 1e-5
+
+
 @pytest.mark.parametrize("forcing", ["none", "const_power", "ekin_tot"])
 def test_step_energy_equals_kinetic_energy(forcing):
     """l3es_step_energy's KE (after ekin_tot rescaling: e_high + alpha^2 e_low) equals
