@@ -13,9 +13,11 @@ its pieces are restated from their published definitions:
     + p_background;
   - neighbor_list(..., mask_self=False): every pair with distance below the cutoff,
     the particle itself included, periodic minimum-image displacements.
-PARITY UNPINNED: no reference output exists for these paths (jax_sph is absent), so
-the restatement is checked only for internal consistency (symmetry, constant density
-on a lattice, momentum conservation).
+Parity: pinned to the reference's own relax.py and utils.rho_computer, run with a
+stand-in for jax_sph whose kernel and EoS are the definitions above
+(tests/golden/make_golden_sph.py; matched to 1e-12 by tests/test_sph_oracle.py).
+jax_sph's own constants remain a restatement, checked for internal consistency
+(symmetry, constant density on a lattice, momentum conservation).
 """
 
 from __future__ import annotations

@@ -4,7 +4,8 @@ Used only by ``make_golden.py`` to run the reference's own source files in a
 container where jax/jaxlib 0.4.29 are not installed. The reference enables x64
 (l3es/spectral_solver.py:24), so FP64 NumPy arithmetic is the same precision.
 Covered: ``jax.numpy`` (delegating to numpy, with ``x.at[idx].set/add``),
-``jax.config``, ``jax.lax.scan``, ``jax.vmap``, ``jax.jit`` (identity) and import
+``jax.config``, ``jax.lax.scan``, ``jax.vmap``, ``jax.jit`` (identity),
+``jax.ops.segment_sum`` and import
 stubs for the unavailable third-party packages (jax_cfd, jax_sph, finufft,
 matplotlib), whose functions are never called on the fixture paths.
 """
@@ -90,6 +91,8 @@ def _vmap(f, in_axes=0):
         for i in range(n):
             sub = [a if ax is None else np.take(a, i, axis=ax) for a, ax in zip(args, axes)]
             outs.append(f(*sub))
+        if isinstance(outs[0], dict):  # a pytree of arrays, as jax.vmap returns it
+            return {k: _wrap(np.stack([o[k] for o in outs])) for k in outs[0]}
         if isinstance(outs[0], tuple):
             return tuple(
                 None if outs[0][j] is None else _wrap(np.stack([o[j] for o in outs]))
@@ -120,6 +123,16 @@ def install() -> None:
     jax.jit = lambda f, *a, **k: f
     jax.random = types.ModuleType("jax.random")
     jax.ops = types.ModuleType("jax.ops")
+
+    def _segment_sum(data, segment_ids, num_segments):
+        data = np.asarray(data)
+        out = np.zeros((num_segments,) + data.shape[1:], dtype=data.dtype)
+        ids = np.asarray(segment_ids)
+        keep = (ids >= 0) & (ids < num_segments)  # jax drops out-of-range ids
+        np.add.at(out, ids[keep], data[keep])
+        return _wrap(out)
+
+    jax.ops.segment_sum = _segment_sum
     jax.lib = types.SimpleNamespace(
         xla_bridge=types.SimpleNamespace(
             get_backend=lambda: types.SimpleNamespace(platform="cpu")

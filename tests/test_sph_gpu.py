@@ -164,3 +164,27 @@ def test_combined_with_relaxation_matches_oracle_loop(tmp_path):
         u_rel = S.relax_velocity(r_o, ur, dt, f, c, 2, u_ref)
         r_o = R.shift_fn(r_o, dt * u_rel)
     assert np.abs(r.cpu().numpy() - r_o).max() < 1e-6
+
+
+@pytest.mark.parametrize("name", ["d2_n16", "d3_n8"])
+def test_sph_matches_reference_golden(gold, name):
+    """Density, relaxation acceleration and the three sph_body terms against the
+    reference's own relax.py / utils.py run with a jax_sph stand-in
+    (tests/golden/make_golden_sph.py)."""
+    from l3es import _native
+    from l3es.relax import relax_wrapper
+
+    c = {k.split("/", 1)[1]: v for k, v in gold("sph").items() if k.startswith(name + "/")}
+    n, dim, u_ref = int(c["n"]), int(c["dim"]), float(c["u_ref"])
+    r, u = c["r"], c["u"]
+    p = _native.SphPlan(dim, n)
+    rho = torch.empty(r.shape[0], dtype=torch.float64, device="cuda")
+    p.density(_dev(r), rho)
+    assert np.abs(rho.cpu().numpy() - c["rho"]).max() < RHO_TOL
+    acc = torch.empty(r.shape, dtype=torch.float64, device="cuda")
+    p.relax_acceleration(_dev(r), acc, u_ref)
+    assert _rel(acc, c["acc_relax"]) < ACC_TOL
+    _, sph_body = relax_wrapper(n, dim, L, is_physical=True, u_ref=u_ref)
+    got = sph_body(r, u)
+    for k in ("acc_p", "acc_visc", "acc_tvf"):
+        assert _rel(got[k], c[k]) < ACC_TOL, k
