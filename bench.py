@@ -439,6 +439,37 @@ def fp64_plain_rate(u0, dt, n, steps, warmup):
 # 1e-3 of a direction with the norm of u_hat0) on seeded random HIT directions, and
 # the FP64 loss. Cost: adjoint step / forward step, CUDA events.
 # ---------------------------------------------------------------------------------
+def adjoint_cost(n, dt, reps=10):
+    """Milliseconds of one forward step and of one adjoint step (l3es_adjoint_step: the
+    three stages recomputed + four VJPs) of the headline HIT workload at n^3."""
+    import torch
+
+    from l3es import _native
+
+    u0, _ = initial_field(n)
+    plan = _native.Plan(dim=3, n=n, nu=NU, dt=dt, forcing="const_power", kf=KF, eps_inj=EPS_INJ)
+    plan.autotune("")
+    uh = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
+    plan.rfftn(torch.from_numpy(u0.astype(np.float32)).cuda(), uh)
+    x, lam = uh.clone(), uh.clone()
+    for _ in range(3):
+        plan.step(x, 1)
+        plan.adjoint_step(uh, lam)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    for _ in range(reps):
+        plan.step(x, 1)
+    ev[1].record()
+    for _ in range(reps):
+        plan.adjoint_step(uh, lam)
+    ev[2].record()
+    torch.cuda.synchronize()
+    plan.check()
+    fwd, adj = ev[0].elapsed_time(ev[1]) / reps, ev[1].elapsed_time(ev[2]) / reps
+    return {"n": n, "fwd_ms_per_step": fwd, "adj_ms_per_step": adj, "adjoint_over_forward": adj / fwd}
+
+
 def adjoint_check(dirs=16, n=128, c=32, steps=20, dt=2e-3, h=1e-3):
     import torch
 
@@ -886,9 +917,24 @@ def run_ours(args):
         ke_host.copy_(ke_dev, non_blocking=True)
         stream.synchronize()
     e2e_sync_ms = (time.perf_counter() - t0) * 1e3 / max(nsteps_e2e, 1)
-    # (b) pipelined: the host reads step i's results (double-buffered pinned outputs, one
-    # event wait per step) while step i+1 runs; the positions still travel device ->
-    # pinned host -> device between steps (stream order), every step
+    # (b) pipelined on two streams: the DNS step (with its KE) on the main stream, the
+    # particle part on a second one: H2D of the positions, coarsening once the step's
+    # field exists, interpolation + advection, D2H of u_r and the new positions. The next
+    # DNS step waits only until the coarsening has read the field, so the interpolation
+    # and the copies of step i run under the DNS of step i+1; the positions still travel
+    # device -> pinned host -> device every step, and the host reads step i's results
+    # (double-buffered pinned outputs, one event wait per step) while step i+1 runs.
+    cap = _native.Graph.begin()
+    plan.step(uh, 1, ke=ke_dev, stream=cap)
+    g_dns = _native.Graph.end(cap)
+    cap = _native.Graph.begin()
+    ip.set_spectrum(uh, stream=cap)
+    g_crop = _native.Graph.end(cap)
+    cap = _native.Graph.begin()
+    ip.interp(r_dev, u_r, backend="nufft", dt=dt, r_out=r_new, stream=cap)
+    g_part = _native.Graph.end(cap)
+    side = torch.cuda.Stream()
+    ev_dns, ev_crop = torch.cuda.Event(), torch.cuda.Event()
     ur_pins = [ur_pin, torch.empty_like(ur_pin).pin_memory()]
     ke_hosts = [ke_host, torch.zeros(1, dtype=torch.float64).pin_memory()]
     evs = [torch.cuda.Event(), torch.cuda.Event()]
@@ -897,12 +943,20 @@ def run_ours(args):
     t0 = time.perf_counter()
     for i in range(nsteps_e2e):
         b = i & 1
-        r_dev.copy_(r_pin, non_blocking=True)
-        g_e2e.launch(stream)
-        ur_pins[b].copy_(u_r, non_blocking=True)
-        r_pin.copy_(r_new, non_blocking=True)
+        if i > 0:
+            stream.wait_event(ev_crop)  # the previous coarsening has read the field
+        g_dns.launch(stream)
         ke_hosts[b].copy_(ke_dev, non_blocking=True)
-        evs[b].record(stream)
+        ev_dns.record(stream)
+        with torch.cuda.stream(side):
+            r_dev.copy_(r_pin, non_blocking=True)  # after the previous step's D2H (same stream)
+            side.wait_event(ev_dns)
+            g_crop.launch(side)
+            ev_crop.record(side)
+            g_part.launch(side)
+            ur_pins[b].copy_(u_r, non_blocking=True)
+            r_pin.copy_(r_new, non_blocking=True)
+            evs[b].record(side)  # also after the KE copy: the side stream waited on ev_dns
         if i > 0:
             evs[b ^ 1].synchronize()
             ke_seen.append(float(ke_hosts[b ^ 1][0]))
@@ -925,6 +979,8 @@ def run_ours(args):
     adjoint = None
     if rank == 0 and not args.skip_baselines and args.adjoint_dirs > 0:
         adjoint = adjoint_check(dirs=args.adjoint_dirs)
+        # the same cost ratio on the headline 256^3 workload (no gradient check there)
+        adjoint["at_headline_size"] = adjoint_cost(n, dt)
     extra = {}
     if rank == 0 and not args.skip_baselines:
         extra["hit_ekin_tot"] = hit_ekin_tot_rate(args.steps, args.warmup)
@@ -968,9 +1024,11 @@ def run_ours(args):
             "e2e": {"value": 1e3 / e2e_ms, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "synced_each_step": 1e3 / e2e_sync_ms,
                     "note": "host-timed through the public API: every step copies the pinned host positions in "
-                            "and the velocities, new positions and KE out; device work is one l3es graph launch; "
-                            "value: the host reads step i's results while step i+1 runs (double-buffered pinned "
-                            "outputs); synced_each_step: the host waits for every step before the next"},
+                            "and the velocities, new positions and KE out; value: the DNS step and the particle "
+                            "part (positions in, coarsening, interpolation + advection, results out) as library "
+                            "graphs on two streams, the particle part and copies of step i under the DNS of step "
+                            "i+1, the host reading step i's results while step i+1 runs; synced_each_step: one "
+                            "graph per step and the host waits for every step before the next"},
             "with_u_out": with_u_out,
             **extra,
             "gpu_launches": launches,
