@@ -1113,27 +1113,28 @@ def run_batch24(args, emit=True):
         pl.set_nu([r["nu"] for r in rs])
         schedules[f"{dim}d_{n}x{count}"] = pl.autotune("")
         uh = torch.stack([spec(pl, r["u"], dim, n) for r in rs]).contiguous()
-        parts = []
+        part = None
         if dim == 2:
-            for b, r in enumerate(rs):
-                ip = _native.InterpPlan(dim=2, ckp_n=32, n_fine=n, np_max=1024)
-                rr = [particles2d(r["seed"]), torch.empty(1024, 2, dtype=torch.float64, device="cuda")]
-                parts.append((ip, b, rr, torch.empty(1024, 2, dtype=torch.float64, device="cuda"), dt))
-        groups.append((pl, uh, parts))
+            # one batched interpolator per size: each particle kernel launches once for the
+            # group's trajectories ([count][1024][2] positions)
+            ip = _native.InterpPlan(dim=2, ckp_n=32, n_fine=n, np_max=1024, batch=count)
+            rr = [torch.stack([particles2d(r["seed"]) for r in rs]).contiguous(),
+                  torch.empty(count, 1024, 2, dtype=torch.float64, device="cuda")]
+            part = (ip, rr, torch.empty(count, 1024, 2, dtype=torch.float64, device="cuda"), dt)
+        groups.append((pl, uh, part))
 
     def record(graph_pingpong):
-        # one graph branch per grid size (its batched DNS step), and one sub-branch per
-        # particle plan after it: the sizes and the particle updates run side by side
+        # one graph branch per grid size: its batched DNS step, then its batched particle
+        # update; the sizes run side by side
         cap = _native.Graph.begin()
-        for pl, uh, parts in groups:
+        for pl, uh, part in groups:
             br = _native.Graph.fork(cap)
             pl.step(uh, 1, stream=br)
-            for ip, b, rr, ur, dt in parts:
-                pb = _native.Graph.fork(br)
-                ip.set_spectrum(uh[b], stream=pb)
+            if part is not None:
+                ip, rr, ur, dt = part
+                ip.set_spectrum(uh, stream=br)
                 src, dst = (rr[0], rr[1]) if graph_pingpong == 0 else (rr[1], rr[0])
-                ip.interp(src, ur, dt=dt, r_out=dst, stream=pb)
-                _native.Graph.join(br, pb)
+                ip.interp(src, ur, dt=dt, r_out=dst, stream=br)
             _native.Graph.join(cap, br)
         return _native.Graph.end(cap)
 
@@ -1191,8 +1192,8 @@ def run_batch24(args, emit=True):
         "vs_baseline": None, "dtype": "f32 (fp64 reductions)", "data": "synthetic",
         "config": {"workload": "batch24: 2D Kolmogorov 8x128^2 + 6x256^2 + 2x512^2 (32^2 particles each), "
                                "3D HIT 6x64^3 + 2x128^3", "grid_points_per_step": points,
-                   "batched": "5 plans (one per size, per-trajectory nu) + 16 particle plans, one CUDA graph per step "
-                              "with one branch per size and per particle plan (concurrent)"},
+                   "batched": "5 step plans (one per size, per-trajectory nu) + 3 batched particle plans (one per 2D "
+                              "size), one CUDA graph per step with one branch per size (concurrent)"},
         "sequential": {"value": seq_rate, "steps": seq_steps, "ms_per_step": 1e3 * t_seq / seq_steps,
                        "note": "24 single-trajectory plans launched one after another"},
         "speedup_vs_sequential": batched_rate / seq_rate,

@@ -190,6 +190,14 @@ typedef struct l3es_interp_plan l3es_interp_plan;
  * width: ES kernel width (4, 6 or 8; upsampling 2); np_max: particle capacity. */
 int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width,
                             int64_t np_max, l3es_interp_plan** out);
+/* Batched interpolator (no counterpart in the reference, which runs one trajectory per
+ * job): `batch` trajectories of the same sizes, np_max particles each. It serves
+ * l3es_interp_set_spectrum with the fine spectra of a batched step plan ([batch][3][...],
+ * contiguous) and l3es_interp with backend 0 (NUFFT) on positions / velocities laid out
+ * [batch][np][dim] (np per trajectory), each kernel launched once for all trajectories;
+ * its other calls return L3ES_EINVAL. Results equal those of one plan per trajectory. */
+int l3es_interp_plan_create_batch(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width,
+                                  int64_t np_max, int32_t batch, l3es_interp_plan** out);
 int l3es_interp_plan_destroy(l3es_interp_plan* plan);
 
 /* Coarse spectrum of spectral_filtering(irfftn(u_hat), ckp_N) taken directly from

@@ -119,15 +119,21 @@ __device__ __forceinline__ int particle_bin(const double* __restrict__ r, long l
   return b;
 }
 
+// Batched plans: trajectory blockIdx.y (blockIdx.x for the scan) has its positions at
+// r + b np dim, its bins at count / start + b nbins and its permutation at perm + b np.
 template <int DIM>
-__global__ void k_bin_count(const double* __restrict__ r, long long np, int nb, int* __restrict__ count) {
+__global__ void k_bin_count(const double* __restrict__ r, long long np, int nb, int nbins, int* __restrict__ count) {
   const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  r += (long long)blockIdx.y * np * DIM;
+  count += (long long)blockIdx.y * nbins;
   if (j < np) atomicAdd(count + particle_bin<DIM>(r, j, nb), 1);
 }
 
 // exclusive scan of nbins counts by one CTA of 1024 threads (chunked)
 __global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ count, int nbins, int* __restrict__ start) {
   __shared__ int part[1024];
+  count += (long long)blockIdx.x * nbins;
+  start += (long long)blockIdx.x * nbins;
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
@@ -150,9 +156,12 @@ __global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ count
 }
 
 template <int DIM>
-__global__ void k_bin_scatter(const double* __restrict__ r, long long np, int nb, int* __restrict__ cursor,
+__global__ void k_bin_scatter(const double* __restrict__ r, long long np, int nb, int nbins, int* __restrict__ cursor,
                               int* __restrict__ perm) {
   const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  r += (long long)blockIdx.y * np * DIM;
+  cursor += (long long)blockIdx.y * nbins;
+  perm += (long long)blockIdx.y * np;
   if (j < np) perm[atomicAdd(cursor + particle_bin<DIM>(r, j, nb), 1)] = (int)j;
 }
 
@@ -174,6 +183,14 @@ k_nufft_gather(const float* __restrict__ gre, long long gcs, int n, int ncomp, f
                const double* __restrict__ r, const int* __restrict__ perm, long long np, double* __restrict__ u_r,
                double dt, double* __restrict__ r_out) {
   static_assert(W <= kGatherLanes, "one support row per lane");
+  {  // batched plans: trajectory blockIdx.y (its 3-field grid, positions, order, outputs)
+    const long long b = blockIdx.y;
+    gre += b * 3 * gcs;
+    r += b * np * DIM;
+    if (perm) perm += b * np;
+    u_r += b * np * ncomp;
+    if (r_out) r_out += b * np * DIM;
+  }
   const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long i = gt / kGatherLanes;
   const int a = (int)(gt % kGatherLanes);
@@ -631,6 +648,7 @@ static void gauss_legendre(int m, std::vector<double>& x, std::vector<double>& w
 
 struct l3es_interp_plan {
   int dim = 3, c = 32, n = 64, w = 6, n_fine = 0;
+  int batch = 1;  // trajectories (batched plans: set_spectrum and the NUFFT interpolation only)
   long long np_max = 0;
   int nb = 16;  // bins per axis
   double beta = 0.0;
@@ -696,15 +714,16 @@ static void grid_passes(const l3es_interp_plan* p, cudaStream_t s) {
   using KY = KyCfg<NG>;
   constexpr int TX = KY::THREADS, TWY = KY::TWY;
   const long long per = p->gcs;
+  const unsigned nf = 3u * (unsigned)p->batch;  // fields of every trajectory, one after another
   if (p->dim == 3) {
     // x: pencils of stride n^2, columns = (y, z) flattened
-    ky_pass<NG, kInv><<<dim3((NG * NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG * NG + TWY - 1) / TWY, 1, nf), TX, 0, s>>>(p->g, per, NG * NG, NG * NG, NG / 2, p->tw);
     // y: pencils of stride n inside each x-plane, columns = z
-    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, NG, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, NG, nf), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
   } else {
-    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, 1, 3), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
+    ky_pass<NG, kInv><<<dim3((NG + TWY - 1) / TWY, 1, nf), TX, 0, s>>>(p->g, per, NG, NG, NG / 2, p->tw);
   }
-  const long long lines = 3 * per / NG;
+  const long long lines = (long long)nf * per / NG;
   constexpr int LPC = (32 / Fft<NG>::T) * 4;
   line_c2c_re<NG><<<(unsigned)((lines + LPC - 1) / LPC), 128, 0, s>>>(p->g, p->gre, lines, p->tw, 1.0f);
 }
@@ -753,8 +772,16 @@ extern "C" {
 
 int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width, int64_t np_max,
                             l3es_interp_plan** out) {
+  return l3es_interp_plan_create_batch(dim, n_fine, ckp_n, width, np_max, 1, out);
+}
+
+int l3es_interp_plan_create_batch(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t width, int64_t np_max,
+                                  int32_t batch, l3es_interp_plan** out) {
   if (!out) return fail(L3ES_EINVAL, "l3es_interp_plan_create: null out");
   *out = nullptr;
+  if (batch < 1) return fail(L3ES_EINVAL, "l3es_interp_plan_create_batch: batch < 1");
+  if (batch > 1 && n_fine <= 0)
+    return fail(L3ES_EINVAL, "l3es_interp_plan_create_batch: a batched plan needs a fine grid (n_fine > 0)");
   if (dim != 2 && dim != 3) return fail(L3ES_EINVAL, "dim must be 2 or 3");
   if (ckp_n != 8 && ckp_n != 16 && ckp_n != 32 && ckp_n != 64 && ckp_n != 128)
     return fail(L3ES_EINVAL, "ckp_N must be 8, 16, 32, 64 or 128");
@@ -769,6 +796,7 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   p->w = width;
   p->n_fine = n_fine;
   p->np_max = np_max;
+  p->batch = batch;
   p->beta = 2.30 * width;
   p->nb = p->n / 4;
   const int hc = ckp_n / 2 + 1;
@@ -777,14 +805,14 @@ int l3es_interp_plan_create(int32_t dim, int32_t n_fine, int32_t ckp_n, int32_t 
   const long long nbins = dim == 3 ? (long long)p->nb * p->nb * p->nb : (long long)p->nb * p->nb;
   int rc = L3ES_OK;
   rc = rc ? rc : ip_alloc(p, (void**)&p->tw, sizeof(float2) * p->n, "twiddles");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->hh, sizeof(float2) * 3 * p->hcs, "coarse spectrum");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->g, sizeof(float2) * 3 * p->gcs, "nufft grid");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->gre, sizeof(float) * 3 * p->gcs, "nufft grid re");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->hh, sizeof(float2) * 3 * batch * p->hcs, "coarse spectrum");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->g, sizeof(float2) * 3 * batch * p->gcs, "nufft grid");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->gre, sizeof(float) * 3 * batch * p->gcs, "nufft grid re");
   rc = rc ? rc : ip_alloc(p, (void**)&p->inv_psi, sizeof(float) * ckp_n, "deconvolution");
   rc = rc ? rc : ip_alloc(p, (void**)&p->twc, sizeof(float2) * ckp_n, "coarse twiddles");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->count, sizeof(int) * nbins, "bins");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * nbins, "bin starts");
-  rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * (np_max > 0 ? np_max : 1), "permutation");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->count, sizeof(int) * batch * nbins, "bins");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->start, sizeof(int) * batch * nbins, "bin starts");
+  rc = rc ? rc : ip_alloc(p, (void**)&p->perm, sizeof(int) * batch * (np_max > 0 ? np_max : 1), "permutation");
   rc = rc ? rc : ip_alloc(p, (void**)&p->red, sizeof(double) * 1024, "loss partials");
   const size_t rk_bytes = sizeof(double) * dim * (np_max > 0 ? np_max : 1);
   rc = rc ? rc : ip_alloc(p, (void**)&p->rk_acc, rk_bytes, "rk4 accumulator");
@@ -857,25 +885,29 @@ int l3es_interp_set_spectrum(l3es_interp_plan* p, const void* u_hat_fine, void* 
   const long long cs = p->dim == 3 ? (long long)N * N * (N / 2 + 1) : (long long)N * (N / 2 + 1);
   const float scale = (float)std::pow((double)c / N, p->dim);
   const unsigned blocks = (unsigned)((p->hcs + 255) / 256);
+  const unsigned nf = 3u * (unsigned)p->batch;  // batched: [batch][3] fine spectra in, [batch][3] coarse out
   if (p->dim == 3)
-    k_crop<3><<<dim3(blocks, 3), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
+    k_crop<3><<<dim3(blocks, nf), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
   else
-    k_crop<2><<<dim3(blocks, 3), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
+    k_crop<2><<<dim3(blocks, nf), 256, 0, s>>>((const float2*)u_hat_fine, cs, N, p->hh, p->hcs, c, scale);
   return cuda_check(cudaGetLastError(), "l3es_interp_set_spectrum launch");
 }
 
 int l3es_interp_set_field(l3es_interp_plan* p, const float* u_coarse, void* stream) {
   if (!p || !u_coarse) return fail(L3ES_EINVAL, "l3es_interp_set_field: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_set_field: not for batched plans");
   return l3es_rfftn(p->coarse, u_coarse, p->hh, stream);
 }
 
 int l3es_interp_coarse_field(l3es_interp_plan* p, float* u_coarse, void* stream) {
   if (!p || !u_coarse) return fail(L3ES_EINVAL, "l3es_interp_coarse_field: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_coarse_field: not for batched plans");
   return l3es_irfftn(p->coarse, p->hh, u_coarse, stream);
 }
 
 int l3es_interp_coarse_spectrum(l3es_interp_plan* p, void* out, void* stream) {
   if (!p || !out) return fail(L3ES_EINVAL, "l3es_interp_coarse_spectrum: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_coarse_spectrum: not for batched plans");
   return cuda_check(cudaMemcpyAsync(out, p->hh, sizeof(float2) * 3 * p->hcs, cudaMemcpyDeviceToDevice,
                                     (cudaStream_t)stream),
                     "l3es_interp_coarse_spectrum");
@@ -906,7 +938,7 @@ static int nufft_eval(l3es_interp_plan* p, const double* r, int64_t np, double* 
   const int ncomp = p->dim;
   const double norm = 1.0 / (std::pow((double)p->n, p->dim) * std::pow((double)p->c, p->dim));
   const float beta = (float)p->beta;
-  const unsigned gblk = (unsigned)((np * kGatherLanes + 127) / 128);
+  const dim3 gblk((unsigned)((np * kGatherLanes + 127) / 128), (unsigned)p->batch);
 #define L3ES_GATHER(D, W)                                                                                   \
   k_nufft_gather<D, W><<<gblk, 128, 0, s>>>(p->gre, p->gcs, p->n, ncomp, beta, norm, r, p->perm, np, u_r, dt, \
                                           r_out)
@@ -932,6 +964,7 @@ int l3es_interp(l3es_interp_plan* p, const double* r, int64_t np, double* u_r, i
   if (!p || !r || !u_r) return fail(L3ES_EINVAL, "l3es_interp: null argument");
   if (np < 0 || np > p->np_max) return fail(L3ES_EINVAL, "l3es_interp: np outside [0, np_max]");
   if (backend != 0 && backend != 1) return fail(L3ES_EINVAL, "l3es_interp: backend must be 0 (nufft) or 1 (dft)");
+  if (p->batch > 1 && backend != 0) return fail(L3ES_EINVAL, "l3es_interp: batched plans interpolate by NUFFT only");
   if (np == 0) return L3ES_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (backend == 1) return dft_eval(p, r, np, u_r, dt, r_out, s);
@@ -947,6 +980,7 @@ int l3es_interp_advect_rk4(l3es_interp_plan* p, const double* r, int64_t np, dou
     return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: backend must be 0 (nufft) or 1 (dft)");
   if (r_out == r || u_r == r || u_r == r_out)
     return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: r, u_r and r_out must be separate arrays");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_advect_rk4: not for batched plans");
   if (np == 0) return L3ES_OK;
   cudaStream_t s = (cudaStream_t)stream;
   int rc = backend == 0 ? nufft_grid(p, r, np, s) : L3ES_OK;  // one grid, bins of r reused by every stage
@@ -972,28 +1006,29 @@ static int bin_particles(l3es_interp_plan* p, const double* r, int64_t np, cudaS
 
 static int nufft_grid(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s) {
   const unsigned gb = (unsigned)((p->gcs + 255) / 256);
+  const unsigned nf = 3u * (unsigned)p->batch;
   if (p->dim == 3)
-    k_nufft_prep<3><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
+    k_nufft_prep<3><<<dim3(gb, nf), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
   else
-    k_nufft_prep<2><<<dim3(gb, 3), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
+    k_nufft_prep<2><<<dim3(gb, nf), 256, 0, s>>>(p->hh, p->hcs, p->c, p->inv_psi, p->g, p->gcs, p->n);
   const int rc = run_grid_passes(p, s);
   return rc != L3ES_OK ? rc : bin_particles(p, r, np, s);
 }
 
 // counting sort of the particles by cell into p->perm
 static int bin_particles(l3es_interp_plan* p, const double* r, int64_t np, cudaStream_t s) {
-  const unsigned pb = (unsigned)((np + 127) / 128);
+  const dim3 pb((unsigned)((np + 127) / 128), (unsigned)p->batch);
   const int nbins = p->dim == 3 ? p->nb * p->nb * p->nb : p->nb * p->nb;
-  int rc = cuda_check(cudaMemsetAsync(p->count, 0, sizeof(int) * nbins, s), "l3es_interp memset");
+  int rc = cuda_check(cudaMemsetAsync(p->count, 0, sizeof(int) * nbins * p->batch, s), "l3es_interp memset");
   if (rc != L3ES_OK) return rc;
   if (p->dim == 3) {
-    k_bin_count<3><<<pb, 128, 0, s>>>(r, np, p->nb, p->count);
-    k_bin_scan<<<1, 1024, 0, s>>>(p->count, nbins, p->start);
-    k_bin_scatter<3><<<pb, 128, 0, s>>>(r, np, p->nb, p->start, p->perm);
+    k_bin_count<3><<<pb, 128, 0, s>>>(r, np, p->nb, nbins, p->count);
+    k_bin_scan<<<p->batch, 1024, 0, s>>>(p->count, nbins, p->start);
+    k_bin_scatter<3><<<pb, 128, 0, s>>>(r, np, p->nb, nbins, p->start, p->perm);
   } else {
-    k_bin_count<2><<<pb, 128, 0, s>>>(r, np, p->nb, p->count);
-    k_bin_scan<<<1, 1024, 0, s>>>(p->count, nbins, p->start);
-    k_bin_scatter<2><<<pb, 128, 0, s>>>(r, np, p->nb, p->start, p->perm);
+    k_bin_count<2><<<pb, 128, 0, s>>>(r, np, p->nb, nbins, p->count);
+    k_bin_scan<<<p->batch, 1024, 0, s>>>(p->count, nbins, p->start);
+    k_bin_scatter<2><<<pb, 128, 0, s>>>(r, np, p->nb, nbins, p->start, p->perm);
   }
   return cuda_check(cudaGetLastError(), "l3es_interp grid launch");
 }
@@ -1003,6 +1038,7 @@ extern "C" {
 int l3es_interp_vjp(l3es_interp_plan* p, const double* r, int64_t np, const double* lam, int32_t backend,
                     void* grad_fine, void* stream) {
   if (!p || !r || !lam || !grad_fine) return fail(L3ES_EINVAL, "l3es_interp_vjp: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_vjp: not for batched plans");
   if (p->n_fine <= 0) return fail(L3ES_ESTATE, "l3es_interp_vjp: plan was created without a fine grid (n_fine = 0)");
   if (np < 0 || np > p->np_max) return fail(L3ES_EINVAL, "l3es_interp_vjp: np outside [0, np_max]");
   if (backend != 0 && backend != 1) return fail(L3ES_EINVAL, "l3es_interp_vjp: backend must be 0 (nufft) or 1 (dft)");
@@ -1070,6 +1106,7 @@ int l3es_interp_vjp(l3es_interp_plan* p, const double* r, int64_t np, const doub
 int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const double* u_r, int64_t np,
                                   float* u_grid, void* stream) {
   if (!p || !r || !u_r || !u_grid) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: not for batched plans");
   if (np < 0) return fail(L3ES_EINVAL, "l3es_interp_particles_to_grid: np < 0");
   cudaStream_t s = (cudaStream_t)stream;
   const int c = p->c;
@@ -1100,6 +1137,7 @@ int l3es_interp_particles_to_grid(l3es_interp_plan* p, const double* r, const do
 int l3es_interp_coarse_mse(l3es_interp_plan* p, const void* u_hat_fine, const float* target, double* loss_dev,
                            void* grad, void* stream) {
   if (!p || !u_hat_fine || !target || !loss_dev) return fail(L3ES_EINVAL, "l3es_interp_coarse_mse: null argument");
+  if (p->batch > 1) return fail(L3ES_EINVAL, "l3es_interp_coarse_mse: not for batched plans");
   if (p->n_fine <= 0) return fail(L3ES_ESTATE, "plan was created without a fine grid (n_fine = 0)");
   if (grad == u_hat_fine) return fail(L3ES_EINVAL, "l3es_interp_coarse_mse: grad must not alias u_hat_fine");
   cudaStream_t s = (cudaStream_t)stream;

@@ -53,6 +53,7 @@ _SIGNATURES = {
     "l3es_kernel_kind_count": (ctypes.c_int32, []),
     "l3es_kernel_kind_name": (ctypes.c_char_p, [_I]),
     "l3es_interp_plan_create": (ctypes.c_int, [_I, _I, _I, _I, ctypes.c_int64, ctypes.POINTER(_P)]),
+    "l3es_interp_plan_create_batch": (ctypes.c_int, [_I, _I, _I, _I, ctypes.c_int64, _I, ctypes.POINTER(_P)]),
     "l3es_interp_plan_destroy": (ctypes.c_int, [_P]),
     "l3es_interp_set_spectrum": (ctypes.c_int, [_P, _P, _P]),
     "l3es_interp_set_field": (ctypes.c_int, [_P, _P, _P]),
@@ -368,13 +369,17 @@ BACKENDS = {"nufft": 0, "dft": 1}
 class InterpPlan:
     """Owns an ``l3es_interp_plan``: coarse spectrum, NUFFT grid, particle bins."""
 
-    def __init__(self, dim: int, ckp_n: int, n_fine: int = 0, width: int = 6, np_max: int = 0):
+    def __init__(self, dim: int, ckp_n: int, n_fine: int = 0, width: int = 6, np_max: int = 0, batch: int = 1):
+        """batch > 1: one plan for `batch` trajectories of a batched step plan
+        (l3es_interp_plan_create_batch): set_spectrum takes their [batch][3][...] fine
+        spectra, interp their [batch][np][dim] positions, NUFFT only."""
         lib = load()
         h = ctypes.c_void_p()
-        _check(lib.l3es_interp_plan_create(int(dim), int(n_fine), int(ckp_n), int(width), int(np_max),
-                                           ctypes.byref(h)), "l3es_interp_plan_create")
+        _check(lib.l3es_interp_plan_create_batch(int(dim), int(n_fine), int(ckp_n), int(width), int(np_max),
+                                                 int(batch), ctypes.byref(h)), "l3es_interp_plan_create_batch")
         self._h, self._lib = h, lib
         self.dim, self.c, self.n_fine, self.width, self.np_max = int(dim), int(ckp_n), int(n_fine), int(width), int(np_max)
+        self.batch = int(batch)
 
     @property
     def coarse_shape(self):
@@ -387,6 +392,14 @@ class InterpPlan:
         return (3, c, c, c // 2 + 1) if self.dim == 3 else (3, c, c // 2 + 1)
 
     def set_spectrum(self, u_hat_fine, stream=None) -> None:
+        import torch
+
+        n = self.n_fine
+        want = self.batch * 3 * n ** (self.dim - 1) * (n // 2 + 1)
+        if n > 0 and (u_hat_fine.dtype != torch.complex64 or u_hat_fine.numel() != want
+                      or not u_hat_fine.is_contiguous()):
+            raise ValueError(f"u_hat_fine must be a contiguous complex64 tensor of {want} values "
+                             f"({self.batch} x 3 fine half spectra of {n})")
         _check(self._lib.l3es_interp_set_spectrum(self._h, _ptr(u_hat_fine), _stream(stream)),
                "l3es_interp_set_spectrum")
 
@@ -409,9 +422,13 @@ class InterpPlan:
 
         if r.dtype != torch.float64 or u_r.dtype != torch.float64:
             raise ValueError("positions and velocities are float64 (np, dim)")
-        if r.shape != u_r.shape or r.shape[-1] != self.dim:
-            raise ValueError(f"expected (np, {self.dim}) arrays")
-        _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[0]), _ptr(u_r), BACKENDS[backend], float(dt),
+        lead = (self.batch,) if self.batch > 1 else ()
+        if (r.shape != u_r.shape or r.shape[-1] != self.dim or r.dim() != 2 + len(lead)
+                or tuple(r.shape[:len(lead)]) != lead or not r.is_contiguous() or not u_r.is_contiguous()):
+            raise ValueError(f"expected contiguous {lead + ('np', self.dim)} arrays")
+        if r_out is not None and (r_out.shape != r.shape or r_out.dtype != torch.float64 or not r_out.is_contiguous()):
+            raise ValueError("r_out must match r")
+        _check(self._lib.l3es_interp(self._h, _ptr(r), int(r.shape[-2]), _ptr(u_r), BACKENDS[backend], float(dt),
                                      _ptr(r_out), _stream(stream)), "l3es_interp")
 
     def advect_rk4(self, r, u_r, dt: float, r_out, backend: str = "nufft", stream=None) -> None:

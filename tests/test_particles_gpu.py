@@ -169,3 +169,33 @@ def test_rk4_advection_rejects_aliased_outputs():
     u = torch.empty_like(r)
     with pytest.raises(RuntimeError, match="separate"):
         p.advect_rk4(r, u, 0.1, r)
+
+
+@pytest.mark.parametrize("dim,n,c,b,np_", [(2, 128, 32, 3, 1024), (3, 64, 16, 2, 600)])
+def test_batched_interp_plan_equals_single_plans(dim, n, c, b, np_):
+    """One batched interpolator (l3es_interp_plan_create_batch) over the [b][3] spectra of
+    a batched step plan gives the same velocities and advected positions, bit for bit,
+    as one interpolator per trajectory; its single-trajectory calls are refused."""
+    from l3es import _native
+
+    rng = np.random.default_rng(dim * 10 + b)
+    shape = (b, 3, n, n, n // 2 + 1) if dim == 3 else (b, 3, n, n // 2 + 1)
+    uh = torch.from_numpy((rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)).cuda()
+    r = torch.from_numpy(rng.uniform(0, 2 * np.pi, (b, np_, dim))).cuda()
+    dt = 1e-3
+    pb = _native.InterpPlan(dim=dim, ckp_n=c, n_fine=n, np_max=np_, batch=b)
+    pb.set_spectrum(uh)
+    ur_b = torch.empty_like(r)
+    rn_b = torch.empty_like(r)
+    pb.interp(r, ur_b, dt=dt, r_out=rn_b)
+    for t in range(b):
+        ps = _native.InterpPlan(dim=dim, ckp_n=c, n_fine=n, np_max=np_)
+        ps.set_spectrum(uh[t].contiguous())
+        ur = torch.empty(np_, dim, dtype=torch.float64, device="cuda")
+        rn = torch.empty_like(ur)
+        ps.interp(r[t].contiguous(), ur, dt=dt, r_out=rn)
+        assert torch.equal(ur, ur_b[t]) and torch.equal(rn, rn_b[t]), t
+    with pytest.raises(RuntimeError, match="NUFFT only"):
+        pb.interp(r, ur_b, backend="dft")
+    with pytest.raises(ValueError):
+        pb.interp(r[0].contiguous(), ur_b[0].contiguous())
