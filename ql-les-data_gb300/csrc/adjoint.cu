@@ -135,8 +135,13 @@ static int adj_prepare(l3es_plan* p) {
     w.allocs.push_back(*b);
   }
   cudaError_t e = cudaMalloc((void**)&w.Y6, 2 * spec);
+  if (e == cudaSuccess) w.allocs.push_back(w.Y6);
+  const size_t wbytes = sizeof(float2) * 6 * (size_t)c.fs * c.batch;  // the size of the plan's W
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+    e = cudaMalloc((void**)&w.Wst[i], wbytes);
+    if (e == cudaSuccess) w.allocs.push_back(w.Wst[i]);
+  }
   if (e == cudaSuccess) {
-    w.allocs.push_back(w.Y6);
     e = cudaMalloc((void**)&w.band, sizeof(double) * 2 * c.batch);
     if (e == cudaSuccess) w.allocs.push_back(w.band);
   }
@@ -209,6 +214,9 @@ int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* str
   static const double b_rk4[3] = {0.5, 0.5, 1.0};
   float2* stage_out[3] = {w.Ua, w.Ub, w.Uc};
   for (int rk = 0; rk < 3; ++rk) {
+    // the stage's u, curl u lines stay in Wst[rk] for the VJP at the same state
+    Ctx cw = c;
+    cw.W = w.Wst[rk];
     EpiParams prm;
     prm.a_dt = (float)(a_rk4[rk] * d.dt);
     prm.b_dt = (float)(b_rk4[rk] * d.dt);
@@ -219,7 +227,7 @@ int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* str
     prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
     prm.rk = rk;
     prm.if_h = 0.f;
-    plan->tab.stage(c, rk == 0 ? U0 : stage_out[rk - 1], U0, stage_out[rk], rk, prm, s);
+    plan->tab.stage(cw, rk == 0 ? U0 : stage_out[rk - 1], U0, stage_out[rk], rk, prm, s);
   }
   if (d.forcing == L3ES_FORCING_EKIN_TOT) {
     // the step ends with the ekin_tot rescaling of the RK4 result u_rk: recompute u_rk
@@ -258,6 +266,7 @@ int l3es_adjoint_step(l3es_plan* plan, const void* u_hat_n, void* lam, void* str
   for (int j = 0; j < 4; ++j) {
     AdjEpi a = adj_epi(plan);
     a.us = us[j];
+    a.wlines = j > 0 ? w.Wst[3 - j] : nullptr;  // Ub, Ua, U0: recomputed above; Uc: not
     a.lam1 = L1;
     if (j == 0) {  // g4 = dt/6 lam1, lam_in = lam1
       a.g = L1;

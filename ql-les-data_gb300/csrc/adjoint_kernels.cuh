@@ -232,6 +232,7 @@ struct AdjEpi {
   float drag;
   int band_kf2;             // constant-power band 0 < |k|^2 <= band_kf2 (0 = off)
   const double* band_adj;   // [batch][2]: s, c
+  const float2* wlines;     // u, curl u lines of us when already computed (else nullptr)
 };
 
 // ------------------------------------------------------------------------------

@@ -276,19 +276,21 @@ struct DnsOps {
     const double A = 8.0 * 3.0 * c.cs * c.batch;  // bytes of one 3-component spectrum
     const unsigned xb = (unsigned)((mc + TW - 1) / TW);
     const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
-    // u and curl u lines of the stage field: the forward RHS's x and y inverse passes
-    x_inverse<DIM>(c, a.us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
+    // u and curl u lines of the stage field: the forward RHS's x and y inverse passes, or
+    // the lines the stage recomputation left (a.wlines)
+    const float2* wuw = a.wlines ? a.wlines : c.W;
+    if (!a.wlines) x_inverse<DIM>(c, a.us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
     L3ES_LAUNCH(c, KK_ADJ_X_INV, 2.0 * A, s,
                 kx_inv_adjproj<N, DIM><<<dim3(xb, c.batch), TX, 0, s>>>(
                     a.g, c.cs, a.gscale, c.kd, Wm, c.fs, c.tw, a.us, a.band_kf2 > 0 ? c.kf : 0, inv_n2d,
                     c.eps_inj, const_cast<double*>(a.band_adj)));
     if (DIM == 3) {
-      y_inv_rhs(c, 11.0 / 3.0 * A, s);
+      if (!a.wlines) y_inv_rhs(c, 11.0 / 3.0 * A, s);
       y_pass<kInv>(c, KK_Y_INV, 2.0 * A, Wm, c.fs, H, N / 2, 3 * c.batch, s);
     }
     L3ES_LAUNCH(c, KK_ADJ_LINE, 5.0 * A, s,
                 line_cross_adj<N><<<dim3(line_blocks(lines), c.batch), L::THREADS, 0, s>>>(
-                    Wm, c.W, c.fs, Y6, c.cs, scale, c.tw, (int)lines));
+                    Wm, wuw, c.fs, Y6, c.cs, scale, c.tw, (int)lines));
     if (DIM == 3) y_pass<kFwd>(c, KK_Y_FWD, 4.0 * A, Y6, c.cs, H, N / 2, 6 * c.batch, s);
     // Y6 (6 fields per trajectory) -> W, as 2 * batch groups of 3 fields
     L3ES_LAUNCH(c, KK_X_FWD_PLAIN, 4.0 * A, s,

@@ -184,6 +184,8 @@ struct AdjWork {
   float2* Y6 = nullptr;   // [batch][6][cs] product spectra
   float2* LAM = nullptr;  // [batch][3][cs] accumulated cotangent
   float2* G = nullptr;    // [batch][3][cs] stage cotangent
+  float2* Wst[3] = {nullptr, nullptr, nullptr};  // [batch][6][fs] u, curl u lines of U0, Ua, Ub, kept
+                                                 // from the stage recomputation for the VJPs
   double* band = nullptr; // [batch][2]
   double* ekin = nullptr; // [batch][3] ekin_tot adjoint: alpha, c_high, c_low
   std::vector<void*> allocs;

@@ -34,8 +34,12 @@ def _spec(plan_cls, dim, n, u):
     return uh
 
 
-@pytest.mark.parametrize("dim,n,forcing", [(3, 32, "ekin_tot"), (3, 32, "const_power"), (2, 64, "none")])
-def test_batched_plan_matches_single_plans(dim, n, forcing):
+@pytest.mark.parametrize("dim,n,forcing,line", [(3, 32, "ekin_tot", None), (3, 32, "const_power", None),
+                                                 (2, 64, "none", None), (2, 256, "none", 2), (2, 256, "none", 3)])
+def test_batched_plan_matches_single_plans(dim, n, forcing, line):
+    """A batched plan equals one plan per trajectory; at 256 also with the radix-16 line
+    passes (line 2, and 3 fed by bulk copies: the trajectory index enters its copy
+    addresses)."""
     from l3es import _native
 
     count, dt, steps = 3, 2e-3, 3
@@ -46,10 +50,14 @@ def test_batched_plan_matches_single_plans(dim, n, forcing):
     singles = []
     for b in range(count):
         p = _native.Plan(dim=dim, n=n, nu=nus[b], dt=dt, e_kin_init=e0s[b], **kw)
+        if line is not None:
+            p.set_schedule({"line_pair": line})
         uh = _spec(_native.Plan, dim, n, us[b])
         p.step(uh, steps)
         singles.append(uh.cpu().numpy())
     pb = _native.Plan(dim=dim, n=n, nu=0.0, dt=dt, batch=count, **kw)
+    if line is not None:
+        pb.set_schedule({"line_pair": line})
     pb.set_nu(nus)
     pb.set_e0(e0s)
     uhb = torch.stack([_spec(_native.Plan, dim, n, u) for u in us]).contiguous()
