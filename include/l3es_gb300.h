@@ -283,7 +283,7 @@ int l3es_shift(const double* r, const double* dr, int64_t n, double scale, doubl
  * const_power (with drag and the Kolmogorov term) and ekin_tot (the kinetic-energy
  * rescaling after each step, spectral_solver.py:82-112, is differentiated: its adjoint
  * recomputes the step's last stage); plans with L3ES_SCHEME_INTEGRATING_FACTOR return
- * L3ES_EINVAL. The first call allocates the plan's adjoint workspace (10 spectra of the
+ * L3ES_EINVAL. The first call allocates the plan's adjoint workspace (16 spectra of the
  * plan's size); l3es_plan_adjoint_prepare does it ahead of time (before any capture). */
 int l3es_plan_adjoint_prepare(l3es_plan* plan);
 
