@@ -12,7 +12,7 @@
 //   k_sph_order    stable order inside each cell (rank by input index), so that neighbour
 //                  sums run in a fixed order and results are bitwise reproducible; stores
 //                  cell-local FP32 coordinates
-//   k_sph_density  rho = m sum_j W(|r_ij|)            (one thread per particle, cell order)
+//   k_sph_density  rho = m sum_j W(|r_ij|)            (kSphLanes lanes per particle, cell order)
 //   k_sph_accel    pressure + transport-velocity (and viscous) accelerations
 // Cells are cubes of side L / floor(n / 3) >= cutoff, so a 3^dim stencil holds every
 // neighbour. Pair geometry is FP32 from cell-local coordinates (offsets below one cell
@@ -29,6 +29,12 @@
 namespace l3es {
 
 constexpr int kSphThreads = 128;
+// Lanes per particle in the neighbour sums: lane q visits candidates q, q + 8, ... of every
+// stencil cell and the lanes' FP64 partial sums are added by a fixed shuffle tree, so the
+// summation order stays fixed (bitwise reproducible). With one thread per particle a 32^3
+// relaxation call kept ~7 warps per SM, each walking ~900 candidates one load after the
+// other.
+constexpr int kSphLanes = 8;
 
 struct SphGeom {
   double L;      // box side
@@ -174,7 +180,8 @@ k_sph_order(const int* __restrict__ perm0, const int* __restrict__ cell, const i
 // is formed from cell-local coordinates and the stencil offset.
 template <int DIM, class F>
 __device__ __forceinline__ void for_neighbours(const float4 xi, const int3 ci, const SphGeom& g,
-                                               const int* __restrict__ start, const float4* __restrict__ xs, F&& f) {
+                                               const int* __restrict__ start, const float4* __restrict__ xs, int lane,
+                                               F&& f) {
   const int R = g.nc >= 3 ? 1 : 0;
   const int nc = g.nc;
   for (int oz = (DIM == 3 ? -R : 0); oz <= (DIM == 3 ? R : 0); ++oz) {
@@ -189,7 +196,7 @@ __device__ __forceinline__ void for_neighbours(const float4 xi, const int3 ci, c
         const int c = DIM == 3 ? (cx * nc + cy) * nc + cz : cx * nc + cy;
         const float px = xi.x - (float)ox * g.cs, py = xi.y - (float)oy * g.cs, pz = xi.z - (float)oz * g.cs;
         const int b = start[c], e = start[c + 1];
-        for (int jj = b; jj < e; ++jj) {
+        for (int jj = b + lane; jj < e; jj += kSphLanes) {
           const float4 xj = xs[jj];
           float dx = px - xj.x, dy = py - xj.y, dz = DIM == 3 ? pz - xj.z : 0.f;
           if (R == 0) {  // one cell: minimum image
@@ -203,6 +210,13 @@ __device__ __forceinline__ void for_neighbours(const float4 xi, const int3 ci, c
       }
     }
   }
+}
+
+// sum of v over the kSphLanes lanes of a particle (fixed order), in every lane
+__device__ __forceinline__ double lanes_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < kSphLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // cell coordinates of the particle at slot i, from its FP64 wrapped position
@@ -224,15 +238,21 @@ __global__ void __launch_bounds__(kSphThreads)
 k_sph_density(const float4* __restrict__ xs, const int* __restrict__ start, const int* __restrict__ perm,
               const double* __restrict__ xw, long long np, SphGeom g, double m_sigma, double p_ref,
               float2* __restrict__ rp, double* __restrict__ rho_out) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  const float4 xi = xs[i];
-  const int3 ci = slot_cell<DIM>(i, perm, xw, g);
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = gt / kSphLanes;
+  const int lane = (int)(gt % kSphLanes);
+  const bool live = i < np;  // every lane stays for the shuffles
   double acc = 0.0;
-  const float inv_h = g.inv_h;
-  for_neighbours<DIM>(xi, ci, g, start, xs, [&](int, float, float, float, float r2) {
-    acc += (double)quintic_w(sqrtf(r2) * inv_h);
-  });
+  if (live) {
+    const float4 xi = xs[i];
+    const int3 ci = slot_cell<DIM>(i, perm, xw, g);
+    const float inv_h = g.inv_h;
+    for_neighbours<DIM>(xi, ci, g, start, xs, lane, [&](int, float, float, float, float r2) {
+      acc += (double)quintic_w(sqrtf(r2) * inv_h);
+    });
+  }
+  acc = lanes_sum(acc);
+  if (!live || lane != 0) return;
   const double rho = m_sigma * acc;
   rp[i] = make_float2((float)rho, (float)(p_ref * (rho - 1.0)));
   if (rho_out) rho_out[perm[i]] = rho;
@@ -265,15 +285,18 @@ struct SphAccelArgs {
 // Relaxation acceleration = acc_p + acc_tvf / 2.
 template <int DIM, int MODE>
 __global__ void __launch_bounds__(kSphThreads) k_sph_accel(SphAccelArgs a, SphGeom g) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.np) return;
-  const float4 xi = a.xs[i];
-  const int3 ci = slot_cell<DIM>(i, a.perm, a.xw, g);
-  const float2 rpi = a.rp[i];
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = gt / kSphLanes;
+  const int lane = (int)(gt % kSphLanes);
+  const bool live = i < a.np;  // every lane stays for the shuffles
+  const long long is = live ? i : 0;
+  const float4 xi = a.xs[is];
+  const int3 ci = slot_cell<DIM>(is, a.perm, a.xw, g);
+  const float2 rpi = a.rp[is];
   const float inv_ri2 = 1.f / (rpi.x * rpi.x);
-  const float4 ui = MODE == kSphForces ? a.us[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 ui = MODE == kSphForces ? a.us[is] : make_float4(0.f, 0.f, 0.f, 0.f);
   double ap[3] = {0.0, 0.0, 0.0}, at[3] = {0.0, 0.0, 0.0}, av[3] = {0.0, 0.0, 0.0};
-  for_neighbours<DIM>(xi, ci, g, a.start, a.xs, [&](int jj, float dx, float dy, float dz, float r2) {
+  if (live) for_neighbours<DIM>(xi, ci, g, a.start, a.xs, lane, [&](int jj, float dx, float dy, float dz, float r2) {
     const float2 rpj = a.rp[jj];
     const float r = sqrtf(r2);
     const float dw = a.grad_scale * quintic_dw(r * g.inv_h);
@@ -292,6 +315,15 @@ __global__ void __launch_bounds__(kSphThreads) k_sph_accel(SphAccelArgs a, SphGe
       ap[0] += cp * dx; ap[1] += cp * dy; ap[2] += cp * dz;
     }
   });
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    ap[d] = lanes_sum(ap[d]);
+    if (MODE == kSphForces) {
+      at[d] = lanes_sum(at[d]);
+      av[d] = lanes_sum(av[d]);
+    }
+  }
+  if (!live || lane != 0) return;
   const long long j = a.perm[i];
   if (MODE == kSphRelaxAcc) {
 #pragma unroll
@@ -380,7 +412,7 @@ static int sph_build(l3es_sph_plan* p, const double* r, const double* u_pred, do
 }
 
 static void sph_density(l3es_sph_plan* p, long long np, double p_ref, double* rho_out, cudaStream_t s) {
-  const unsigned pb = (unsigned)((np + kSphThreads - 1) / kSphThreads);
+  const unsigned pb = (unsigned)((np * kSphLanes + kSphThreads - 1) / kSphThreads);
   const double m_sigma = p->mass * p->sigma;
   if (p->dim == 3)
     k_sph_density<3><<<pb, kSphThreads, 0, s>>>(p->xs, p->start, p->perm, p->xw, np, p->g, m_sigma, p_ref, p->rp,
@@ -392,7 +424,7 @@ static void sph_density(l3es_sph_plan* p, long long np, double p_ref, double* rh
 
 template <int MODE>
 static void sph_accel(l3es_sph_plan* p, SphAccelArgs& a, cudaStream_t s) {
-  const unsigned pb = (unsigned)((a.np + kSphThreads - 1) / kSphThreads);
+  const unsigned pb = (unsigned)((a.np * kSphLanes + kSphThreads - 1) / kSphThreads);
   if (p->dim == 3)
     k_sph_accel<3, MODE><<<pb, kSphThreads, 0, s>>>(a, p->g);
   else
