@@ -16,8 +16,10 @@
 //   k_sph_accel    pressure + transport-velocity (and viscous) accelerations
 // Cells are cubes of side L / floor(n / 3) >= cutoff, so a 3^dim stencil holds every
 // neighbour. Pair geometry is FP32 from cell-local coordinates (offsets below one cell
-// side, so the FP32 rounding of a pair distance is ~1e-7 of dx); sums over neighbours
-// and the density-to-pressure step (rho - 1) are FP64.
+// side, so the FP32 rounding of a pair distance is ~1e-7 of dx); each lane sums its
+// neighbours' FP32 terms in float-float (Ff, error-free FP32 additions: FP64 arithmetic
+// is scarce on this GPU and FP64 accumulators kept its FP64 pipe 73-85% busy), the lanes
+// combine in FP64, and the density-to-pressure step (rho - 1) is FP64.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -242,16 +244,16 @@ k_sph_density(const float4* __restrict__ xs, const int* __restrict__ start, cons
   const long long i = gt / kSphLanes;
   const int lane = (int)(gt % kSphLanes);
   const bool live = i < np;  // every lane stays for the shuffles
-  double acc = 0.0;
+  Ff part{0.f, 0.f};
   if (live) {
     const float4 xi = xs[i];
     const int3 ci = slot_cell<DIM>(i, perm, xw, g);
     const float inv_h = g.inv_h;
     for_neighbours<DIM>(xi, ci, g, start, xs, lane, [&](int, float, float, float, float r2) {
-      acc += (double)quintic_w(sqrtf(r2) * inv_h);
+      part = ff_add(part, quintic_w(sqrtf(r2) * inv_h));
     });
   }
-  acc = lanes_sum(acc);
+  const double acc = lanes_sum((double)part.hi + (double)part.lo);
   if (!live || lane != 0) return;
   const double rho = m_sigma * acc;
   rp[i] = make_float2((float)rho, (float)(p_ref * (rho - 1.0)));
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kSphThreads) k_sph_accel(SphAccelArgs a, SphGe
   const float2 rpi = a.rp[is];
   const float inv_ri2 = 1.f / (rpi.x * rpi.x);
   const float4 ui = MODE == kSphForces ? a.us[is] : make_float4(0.f, 0.f, 0.f, 0.f);
-  double ap[3] = {0.0, 0.0, 0.0}, at[3] = {0.0, 0.0, 0.0}, av[3] = {0.0, 0.0, 0.0};
+  Ff fp[3] = {}, ft[3] = {}, fv[3] = {};
   if (live) for_neighbours<DIM>(xi, ci, g, a.start, a.xs, lane, [&](int jj, float dx, float dy, float dz, float r2) {
     const float2 rpj = a.rp[jj];
     const float r = sqrtf(r2);
@@ -305,22 +307,25 @@ __global__ void __launch_bounds__(kSphThreads) k_sph_accel(SphAccelArgs a, SphGe
     const float s = dw / (r + a.eps);
     if (MODE == kSphForces) {
       const float cp = -pref * pij * s, ct = -pref * a.p_ref * s;
-      ap[0] += cp * dx; ap[1] += cp * dy; ap[2] += cp * dz;
-      at[0] += ct * dx; at[1] += ct * dy; at[2] += ct * dz;
+      fp[0] = ff_add(fp[0], cp * dx); fp[1] = ff_add(fp[1], cp * dy); fp[2] = ff_add(fp[2], cp * dz);
+      ft[0] = ff_add(ft[0], ct * dx); ft[1] = ff_add(ft[1], ct * dy); ft[2] = ff_add(ft[2], ct * dz);
       const float4 uj = a.us[jj];
       const float cv = pref * s;
-      av[0] += cv * (ui.x - uj.x); av[1] += cv * (ui.y - uj.y); av[2] += cv * (ui.z - uj.z);
+      fv[0] = ff_add(fv[0], cv * (ui.x - uj.x));
+      fv[1] = ff_add(fv[1], cv * (ui.y - uj.y));
+      fv[2] = ff_add(fv[2], cv * (ui.z - uj.z));
     } else {
       const float cp = -pref * (pij + 0.5f * a.p_ref) * s;
-      ap[0] += cp * dx; ap[1] += cp * dy; ap[2] += cp * dz;
+      fp[0] = ff_add(fp[0], cp * dx); fp[1] = ff_add(fp[1], cp * dy); fp[2] = ff_add(fp[2], cp * dz);
     }
   });
+  double ap[3], at[3] = {0.0, 0.0, 0.0}, av[3] = {0.0, 0.0, 0.0};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    ap[d] = lanes_sum(ap[d]);
+    ap[d] = lanes_sum((double)fp[d].hi + (double)fp[d].lo);
     if (MODE == kSphForces) {
-      at[d] = lanes_sum(at[d]);
-      av[d] = lanes_sum(av[d]);
+      at[d] = lanes_sum((double)ft[d].hi + (double)ft[d].lo);
+      av[d] = lanes_sum((double)fv[d].hi + (double)fv[d].lo);
     }
   }
   if (!live || lane != 0) return;
