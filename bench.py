@@ -47,8 +47,8 @@ TRAFFIC_JSON = os.path.join(ROOT, "profiles", "dram_traffic_hit256.json")
 # kernel kinds of the library's timer -> name prefixes of their 256^3 launches in ncu
 TRAFFIC_KERNELS = {"line_cross": ("line_cross<256", "line_cross2<256", "line_cross3<256"),
                    "ky_pass_inv": ("ky_inv_rhs<256",),
-                   "kx_inv_curl": ("kx_inv_tma<256, 1, 1>", "kx_inv_tma<256, true, true>",
-                                   "kx_inv<256, 3, 1, 1>", "kx_inv<256, 3, true, true>"),
+                   "kx_inv_curl": ("kx_inv_tma<256, 1, 1", "kx_inv_tma<256, true, true",
+                                   "kx_inv<256, 3, 1, 1", "kx_inv<256, 3, true, true"),
                    "rk_update": ("k_rk_update<256", "k_rk_update_lin<256"),
                    "kx_fwd_band": ("kx_fwd_band<256", "kx_fwd_band_tma<256"),
                    "ky_pass_fwd": ("ky_pass<256, (int)-1", "ky_pass<256, -1")}
@@ -788,7 +788,11 @@ def run_ours(args):
     n = args.n
     u0, dt = initial_field(n)
     plan = _native.Plan(dim=3, n=n, nu=NU, dt=dt, forcing="const_power", kf=KF, eps_inj=EPS_INJ)
-    schedule = plan.autotune("")  # the library's autotuner, timed fresh (no cache file)
+    if args.schedule is not None:
+        plan.set_schedule(dict(zip(plan.SCHEDULE_KEYS, args.schedule)))
+        schedule = plan.schedule
+    else:
+        schedule = plan.autotune("")  # the library's autotuner, timed fresh (no cache file)
     uh = torch.empty(plan.spec_shape, dtype=torch.complex64, device="cuda")
     u_dev = torch.from_numpy(u0.astype(np.float32)).cuda()
     plan.rfftn(u_dev, uh)
@@ -1229,7 +1233,16 @@ def main():
                          "(--traffic-out) that the headline's roofline.traffic reads")
     ap.add_argument("--traffic-out", default=TRAFFIC_JSON)
     ap.add_argument("--traffic-command", default="", help="the ncu command that made NCU_CSV (stored in the record)")
+    ap.add_argument("--schedule", default=None, metavar="X,Y,LINE,BAND",
+                    help="set the 256^3 plan's kernel schedule (x_bulk,y_radix8,line_pair,band_bulk) instead of "
+                         "autotuning it: profiling runs under ncu, whose serialised launches would steer the "
+                         "autotuner elsewhere, use the schedule the plain run chose")
     args = ap.parse_args()
+    if args.schedule is not None:
+        vals = [int(v) for v in args.schedule.split(",")]
+        if len(vals) != 4:
+            ap.error("--schedule takes four comma-separated integers")
+        args.schedule = vals
     if args.record_traffic:
         rec = record_traffic(args.record_traffic, args.traffic_out, args.traffic_command)
         print(json.dumps({k: v["traffic_per_launch"] for k, v in rec["kernels"].items()}))

@@ -16,6 +16,9 @@
 //   kx_fwd_band  x-axis forward c2c on the kept band, dealias mask, Leray projection
 //                (and the constant-power band coefficient of the stage field)
 //   k_rk_update  elementwise viscosity, extension terms and RK4 stage combination
+// The default explicit step has no elementwise pass: kx_fwd_band combines the stages
+// on the band in place, and the next stage's kx_inv scales every other mode by the
+// closed form of its linear decay (XLin, BandRk).
 // Intermediate fields never exist in physical space in HBM.
 #pragma once
 
@@ -76,6 +79,77 @@ __device__ __forceinline__ void kvec(int kx, int km, int kh, float& k0, float& k
   }
 }
 
+// Closed-form RK4 of a mode whose right-hand side is exactly -(nu k^2 + drag) u (no
+// nonlinear or forcing term), z = (nu k^2 + drag) dt: the field that stage rk writes is
+// a polynomial in z times the step's initial state u0,
+//   rk 0: 1 - z/2               rk 1: 1 - z/2 + z^2/4
+//   rk 2: 1 - z + z^2/2 - z^3/4 rk 3: 1 - z + z^2/2 - z^3/6 + z^4/24 (the new state)
+__device__ __forceinline__ float lin_stage_factor(int rk, float z) {
+  if (rk == 0) return fmaf(-0.5f, z, 1.f);
+  if (rk == 1) return fmaf(z, fmaf(0.25f, z, -0.5f), 1.f);
+  if (rk == 2) return fmaf(z, fmaf(z, fmaf(-0.25f, z, 0.5f), -1.f), 1.f);
+  return fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.f / 24.f, -1.f / 6.f), 0.5f), -1.f), 1.f);
+}
+
+// RK4 step with the stage combination fused into the band pass (kx_fwd_band FUSED):
+// the band B = {|kx| <= kd, |kmid| <= kd (3D), khalf < kt} holds the nonlinear and
+// forcing terms, and its stage fields are written in place into the state S; every
+// other mode keeps the step's initial value u0 in S during the step. The x inverse of
+// stage rk (> 0) reads S and scales a mode outside B by lin_stage_factor(rk - 1, z) on
+// the fly, so that mode is neither read nor written by an elementwise update; the last
+// stage's x inverse also writes its new state lin_stage_factor(3, z) u0 back to S.
+struct XLin {
+  float2* S;                 // the state (the x pass's input), [batch][3][cs]
+  long long cs;
+  const float* nu_b;         // per-trajectory viscosity
+  float drag, dt;
+  int kd, kt, rk;            // rk 0 passes u0 through unscaled
+  int band_kf;               // > 0: block 0 of each trajectory computes the constant-power
+  double inv_n2d, eps_inj;   //   coefficient of the stage field into band_scale
+  double* band_scale;
+};
+
+template <int DIM>
+__device__ __forceinline__ void band_coefficient(const float2* __restrict__ ub, long long cs, int N, int kf,
+                                                 double inv_n2d, double eps_inj, double tiny, double* out);
+
+// Scale the outside-B modes of one x-pass column tile (a[c][e]: x row t + T e of column
+// m = mid * H + kh) to stage rk's field; the last stage stores their new state to S.
+template <int N, int DIM>
+__device__ __forceinline__ void xlin_scale(float2 (&a)[3][Fft<N>::E], int t, int m, const XLin& xl, int batch,
+                                           int* __restrict__ err) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
+  constexpr int MC = (DIM == 3 ? N : 1) * H;
+  const int mid = DIM == 3 ? m / H : 0;
+  const int kh = m - mid * H;
+  const int km = DIM == 3 ? kfull(mid, N) : 0;
+  const unsigned ukd = 2u * (unsigned)xl.kd;
+  const bool colband = (unsigned)(km + xl.kd) <= ukd && kh < xl.kt;
+  const float nu = xl.nu_b[batch];
+  const int k2c = km * km + kh * kh;
+  bool bad = false;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int kx = kfull(t + T * e, N);
+    if (colband && (unsigned)(kx + xl.kd) <= ukd) continue;
+    const float z = (nu * (float)(kx * kx + k2c) + xl.drag) * xl.dt;
+    if (xl.rk == 3) {
+      const float g = lin_stage_factor(3, z);
+      float2* dst = xl.S + (long long)batch * 3 * xl.cs + (long long)(t + T * e) * MC + m;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 nv = make_float2(g * a[c][e].x, g * a[c][e].y);
+        dst[c * xl.cs] = nv;
+        bad |= !isfinite(nv.x + nv.y);
+      }
+    }
+    const float f = lin_stage_factor(xl.rk - 1, z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a[c][e] = make_float2(f * a[c][e].x, f * a[c][e].y);
+  }
+  if (bad) atomicOr(err, kErrNonFinite);
+}
+
 // ------------------------------------------------------------------------------
 // x-axis inverse pass. Columns m in [0, NMID*H) of each x-plane; CURL adds the
 // three components of i k x u_hat (np.cross(kkk, u_hat) * 1j) as fields 3..5.
@@ -128,10 +202,12 @@ __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, 
   }
 }
 
-template <int N, int DIM, bool CURL, bool SKIPWX = false>
+// LINF: the x inverse of a band-fused RK stage (XLin).
+template <int N, int DIM, bool CURL, bool SKIPWX = false, bool LINF = false>
 __global__ void __launch_bounds__(TW * Fft<N>::T)
 kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long long fs,
-       const float2* __restrict__ tw, float2* __restrict__ wx = nullptr) {
+       const float2* __restrict__ tw, float2* __restrict__ wx = nullptr, XLin xl = XLin{},
+       int* __restrict__ err = nullptr) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
@@ -141,12 +217,20 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
   const int m = blockIdx.x * TW + p;
   const bool ok = m < MC;
   const long long bofs = (long long)blockIdx.y * 3 * cs;  // batch of trajectories
+  if constexpr (LINF) {
+    if (xl.band_kf > 0 && blockIdx.x == 0)
+      band_coefficient<DIM>(uh + bofs, cs, N, xl.band_kf, xl.inv_n2d, xl.eps_inj, 1e-30,
+                            xl.band_scale + blockIdx.y);
+  }
   float2 a[3][E];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int e = 0; e < E; ++e)
       a[c][e] = ok ? uh[bofs + c * cs + (long long)(t + T * e) * MC + m] : make_float2(0.f, 0.f);
+  if constexpr (LINF) {
+    if (ok && xl.rk > 0) xlin_scale<N, DIM>(a, t, m, xl, (int)blockIdx.y, err);
+  }
   kx_inv_fields<N, DIM, CURL, SKIPWX>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw, wx,
                                       (long long)blockIdx.y * 2 * fs);
 }
@@ -166,10 +250,11 @@ struct KxTma {
   static constexpr unsigned BYTES = (unsigned)STAGE * sizeof(float2);
 };
 
-template <int N, bool CURL, bool SKIPWX = false>
+template <int N, bool CURL, bool SKIPWX = false, bool LINF = false>
 __global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
 kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, long long fs,
-           const float2* __restrict__ tw, int ntiles, int* __restrict__ err, float2* __restrict__ wx) {
+           const float2* __restrict__ tw, int ntiles, int* __restrict__ err, float2* __restrict__ wx,
+           const __grid_constant__ XLin xl) {
   using K = KxTma<N>;
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
   constexpr int NF = CURL ? 6 : 3;
@@ -179,6 +264,11 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
   __shared__ uint64_t bar;
   const int p = threadIdx.x % TW, t = threadIdx.x / TW;
   const int batch = blockIdx.y;
+  if constexpr (LINF) {
+    if (xl.band_kf > 0 && blockIdx.x == 0)
+      band_coefficient<3>(xl.S + (long long)batch * 3 * xl.cs, xl.cs, N, xl.band_kf, xl.inv_n2d, xl.eps_inj, 1e-30,
+                          xl.band_scale + batch);
+  }
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     mbar_init_fence();
@@ -218,6 +308,9 @@ kx_inv_tma(const __grid_constant__ CUtensorMap umap, float2* __restrict__ w, lon
     if (threadIdx.x == 0 && next < ntiles) {
       fence_proxy_async_smem();
       issue(next);
+    }
+    if constexpr (LINF) {
+      if (xl.rk > 0) xlin_scale<N, 3>(a, t, tile * TW + p, xl, batch, err);
     }
     kx_inv_fields<N, 3, CURL, SKIPWX>(a, t, tile * TW + p, true, sm + p, w, (long long)batch * NF * fs, fs, tw,
                                       wx, (long long)batch * 2 * fs);
@@ -1092,6 +1185,7 @@ struct EpiParams {
   float dt = 0.f;    // the step (used with lin)
   int lin = 0;       // explicit RK4 step whose forcing lies inside the stage region: modes
                      // outside it take the closed form of their linear decay (k_rk_update)
+  int band_rk = 0;   // explicit RK4 step combined inside the band pass (XLin, BandRk)
 };
 
 // Float-float (hi + lo) accumulator: error-free FP32 additions (Knuth's TwoSum, then
@@ -1153,169 +1247,13 @@ __device__ __forceinline__ void block_sum_store_ff(Ff v, double* partial, int bl
   }
 }
 
-// ------------------------------------------------------------------------------
-// x-axis forward pass of the nonlinear term on the dealiased band only
-// (spectral_solver.py:55-58: du *= dealias; du -= (sum du.k/k^2) k). CTA = (half-axis
-// tile inside kt, middle-axis row inside the band). Output P keeps only the kept
-// modes: P[c][kx + kd][kmid + kd][kh] (3D), P[c][kx + kd][kh] (2D), kh < kt, with
-// zeros for kh > kd.
-// ------------------------------------------------------------------------------
-// One tile of kx_fwd_band: d[c][e] = DU component c at x row t + T e of column kh of
-// middle row kmb (band index); x forward FFT, dealias mask, Leray projection into P.
-template <int N, int DIM>
-__device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int t, int kh, int kmb, int kd, int kt,
-                                                 float2* sm, float2* __restrict__ P, long long pcs, long long bp,
-                                                 const float2* __restrict__ tw) {
-  constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  const int nb = 2 * kd + 1;
-  const int km = DIM == 3 ? kmb - kd : 0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    block_fft<N, E, kFwd, TW>(d[c], sm, t, tw, 1);
-    __syncthreads();
-  }
-#pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int kx = kfull(t + T * e, N);
-    if ((unsigned)(kx + kd) > 2u * (unsigned)kd) continue;  // |kx| > kd
-    float k0, k1, k2;
-    kvec<DIM>(kx, km, kh, k0, k1, k2);
-    const bool keep = kh <= kd;
-    const int ik2 = kx * kx + km * km + kh * kh;
-    const float inv = 1.0f / (ik2 == 0 ? 1.0f : (float)ik2);
-    const float2 v0 = keep ? d[0][e] : make_float2(0.f, 0.f);
-    const float2 v1 = keep ? d[1][e] : make_float2(0.f, 0.f);
-    const float2 v2 = keep ? d[2][e] : make_float2(0.f, 0.f);
-    const float pr = (v0.x * k0 + v1.x * k1 + v2.x * k2) * inv;
-    const float pi_ = (v0.y * k0 + v1.y * k1 + v2.y * k2) * inv;
-    const long long o = bp + ((long long)(kx + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
-    P[o] = make_float2(v0.x - pr * k0, v0.y - pi_ * k0);
-    P[o + pcs] = make_float2(v1.x - pr * k1, v1.y - pi_ * k1);
-    P[o + 2 * pcs] = make_float2(v2.x - pr * k2, v2.y - pi_ * k2);
-  }
-}
-
-template <int N, int DIM>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
-kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
-            const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
-            double inv_n2d, double eps_inj, double* __restrict__ band_scale) {
-  constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  constexpr int NMID = DIM == 3 ? N : 1;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
-  const int km = DIM == 3 ? kmb - kd : 0;
-  const int mid = km < 0 ? km + N : km;
-  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
-  const int batch = blockIdx.z;
-  const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
-  if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
-    band_coefficient<DIM>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30,
-                          band_scale + batch);
-  float2 d[3][E];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
-  kx_fwd_band_tile<N, DIM>(d, t, kh, kmb, kd, kt, sm + p, P, pcs, bp, tw);
-}
-
-// Persistent 3D variant of kx_fwd_band: tiles (column tile, band row kmb) are walked
-// blockIdx.x, + gridDim.x, ...; the next tile's DU block (TW columns x N x rows x 3
-// components at middle row `mid`) arrives by one 4D bulk tensor load while the current
-// one is transformed. dmap: DU as (kt, N mid, N x, 3 * batch), box (TW, 1, min(N, 256), 3).
-template <int N>
-__global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
-kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2* __restrict__ P, long long pcs,
-                const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
-                double inv_n2d, double eps_inj, double* __restrict__ band_scale, int* __restrict__ err) {
-  using K = KxTma<N>;
-  constexpr int E = Fft<N>::E, T = Fft<N>::T;
-  extern __shared__ __align__(128) float2 s_dyn[];
-  float2* stage = s_dyn;
-  float2* sm = s_dyn + K::STAGE;
-  __shared__ uint64_t bar;
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int batch = blockIdx.y;
-  const int ntx = kt / TW, nb = 2 * kd + 1, ntiles = ntx * nb;
-  if (band_kf > 0 && blockIdx.x == 0)
-    band_coefficient<3>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30, band_scale + batch);
-  if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
-    mbar_init_fence();
-  }
-  __syncthreads();
-  auto issue = [&](int tile) {
-    const int kmb = tile / ntx, x0 = (tile % ntx) * TW;
-    const int km = kmb - kd, mid = km < 0 ? km + N : km;
-    mbar_arrive_expect_tx(&bar, K::BYTES);
-#pragma unroll
-    for (int l = 0; l < K::LOADS; ++l)
-      tma_load_4d(stage + l * 3 * K::NY * TW, &dmap, &bar, x0, mid, l * K::NY, 3 * batch);
-  };
-  int tile = blockIdx.x;
-  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
-  unsigned parity = 0;
-  for (; tile < ntiles; tile += gridDim.x) {
-    const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;  // as in kx_inv_tma
-    if (__syncthreads_or(!got)) {
-      if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
-      mbar_wait(&bar, parity);
-      return;
-    }
-    if (threadIdx.x >= 32) mbar_wait(&bar, parity);
-    parity ^= 1u;
-    float2 d[3][E];
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const int row = t + T * e;
-        d[c][e] = stage[(((row / K::NY) * 3 + c) * K::NY + row % K::NY) * TW + p];
-      }
-    __syncthreads();
-    const int next = tile + gridDim.x;
-    if (threadIdx.x == 0 && next < ntiles) {
-      fence_proxy_async_smem();
-      issue(next);
-    }
-    kx_fwd_band_tile<N, 3>(d, t, (tile % ntx) * TW + p, tile / ntx, kd, kt, sm + p, P, pcs,
-                           (long long)batch * 3 * pcs, tw);
-  }
-}
-
-// ------------------------------------------------------------------------------
-// Elementwise linear terms + RK4 stage combination (spectral_solver.py:59, :74-80),
-// two complex values (one float4) per thread over all 3 components:
-//   du = P(k) (kept band, else 0) - nu k^2 us [- drag us + forcing terms]
-//   rk 0   : out <- us + b dt du                               (us = u0; no acc)
-//   rk 1   : acc <- u0 + (a0/b0)(us - u0) + a dt du, out <- u0 + b dt du
-//   rk 2   : acc += a dt du,       out <- u0 + b dt du         (us aliases out)
-//   rk 3   : fin <- acc + a dt du
-//   rk -1  : out <- du (the reference's rhs_fn)
-// Every thread loads all its operands before storing (us/out and acc alias).
-// VIF: the integrating-factor form (a separate instantiation, so the reference's explicit
-// form keeps its own code).
-// ------------------------------------------------------------------------------
-// rk_core: one mode given its indices (kxi, mid, kh: storage indices on the x, middle
-// and half axes; kx, km: their signed wavenumbers); rk_elem: by flat index i.
+// rk_core_r: the right-hand side of one mode from its projected nonlinear term r (zero
+// outside the kept band) and the stage combination (ik2 = |k|^2 as an integer).
 template <int N, int DIM, bool VIF = false>
-__device__ __forceinline__ float2 rk_core(int kxi, int mid, int kh, int kx, int km, int c, float2 sv, float2 a0,
-                                          float2 z0, const float2* __restrict__ P, long long pcs, int kt, int kd,
-                                          const EpiParams& prm, float fscale, float2& nv) {
-  const int ik2 = kx * kx + km * km + kh * kh;
+__device__ __forceinline__ float2 rk_core_r(int kxi, int mid, int kh, int ik2, int c, float2 r, float2 sv, float2 a0,
+                                            float2 z0, const EpiParams& prm, float fscale, float2& nv) {
   const float kk2 = (float)ik2;
   const float nu = prm.nu;
-  float2 r = make_float2(0.f, 0.f);
-  // band rows as unsigned offsets: in the band iff 0 <= k + kd <= 2 kd on every axis
-  const unsigned nb = 2u * (unsigned)kd + 1u;
-  const unsigned bx = (unsigned)(kx + kd);
-  const unsigned bm = DIM == 3 ? (unsigned)(km + kd) : 0u;
-  if (bx < nb && bm < nb && (unsigned)kh <= (unsigned)kd) {
-    const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
-    r = __ldg(P + c * pcs + row * kt + kh);
-  }
   const bool vif = VIF && prm.rk >= 0;
   if (!vif) {
     r.x -= nu * kk2 * sv.x;
@@ -1377,6 +1315,226 @@ __device__ __forceinline__ float2 rk_core(int kxi, int mid, int kh, int kx, int 
   }
   nv = make_float2(fmaf(prm.a_dt, r.x, a0.x), fmaf(prm.a_dt, r.y, a0.y));
   return nv;
+}
+
+// Band-fused RK step (XLin): the band pass combines the stages itself. P holds the
+// step's initial state on the band (written at rk 0) and acc the accumulator, both in
+// P's compact layout; S is updated in place on the band.
+struct BandRk {
+  float2* S;
+  float2* acc;
+  long long cs;
+  EpiParams prm;
+  const double* band_scale;
+  const float* nu_b;
+  int* err;
+};
+
+// ------------------------------------------------------------------------------
+// x-axis forward pass of the nonlinear term on the dealiased band only
+// (spectral_solver.py:55-58: du *= dealias; du -= (sum du.k/k^2) k). CTA = (half-axis
+// tile inside kt, middle-axis row inside the band). Output P keeps only the kept
+// modes: P[c][kx + kd][kmid + kd][kh] (3D), P[c][kx + kd][kh] (2D), kh < kt, with
+// zeros for kh > kd.
+// ------------------------------------------------------------------------------
+// One tile of kx_fwd_band: d[c][e] = DU component c at x row t + T e of column kh of
+// middle row kmb (band index); x forward FFT, dealias mask, Leray projection into P.
+template <int N, int DIM, bool FUSED = false>
+__device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int t, int kh, int kmb, int kd, int kt,
+                                                 float2* sm, float2* __restrict__ P, long long pcs, long long bp,
+                                                 const float2* __restrict__ tw, const BandRk* br = nullptr,
+                                                 int batch = 0) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T, H = N / 2 + 1;
+  constexpr int NMID = DIM == 3 ? N : 1;
+  const int nb = 2 * kd + 1;
+  const int km = DIM == 3 ? kmb - kd : 0;
+  const int mid = km < 0 ? km + N : km;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    block_fft<N, E, kFwd, TW>(d[c], sm, t, tw, 1);
+    __syncthreads();
+  }
+  EpiParams prm;
+  float fscale = 0.f;
+  if constexpr (FUSED) {
+    prm = br->prm;
+    prm.nu = br->nu_b[batch];
+    fscale = prm.band_kf2 > 0 ? (float)br->band_scale[batch] : 0.f;
+  }
+  bool bad = false;
+  // (kt can exceed the half axis only at N = 8: those columns hold no mode of S)
+  const bool live = !FUSED || kh < H;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int kx = kfull(t + T * e, N);
+    if ((unsigned)(kx + kd) > 2u * (unsigned)kd || !live) continue;  // |kx| > kd
+    float k0, k1, k2;
+    kvec<DIM>(kx, km, kh, k0, k1, k2);
+    const bool keep = kh <= kd;
+    const int ik2 = kx * kx + km * km + kh * kh;
+    const float inv = 1.0f / (ik2 == 0 ? 1.0f : (float)ik2);
+    const float2 v0 = keep ? d[0][e] : make_float2(0.f, 0.f);
+    const float2 v1 = keep ? d[1][e] : make_float2(0.f, 0.f);
+    const float2 v2 = keep ? d[2][e] : make_float2(0.f, 0.f);
+    const float pr = (v0.x * k0 + v1.x * k1 + v2.x * k2) * inv;
+    const float pi_ = (v0.y * k0 + v1.y * k1 + v2.y * k2) * inv;
+    const long long o = bp + ((long long)(kx + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
+    const float2 pv[3] = {make_float2(v0.x - pr * k0, v0.y - pi_ * k0), make_float2(v1.x - pr * k1, v1.y - pi_ * k1),
+                          make_float2(v2.x - pr * k2, v2.y - pi_ * k2)};
+    if constexpr (!FUSED) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) P[o + c * pcs] = pv[c];
+    } else {
+      // the stage combination of rk_core on this band mode, in place in S; P holds the
+      // step's initial band values (written at rk 0), br->acc the accumulator
+      const int row = t + T * e;
+      float2* sp = br->S + (long long)batch * 3 * br->cs + ((long long)row * NMID + mid) * H + kh;
+      float2 sv[3], z0[3], a0[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sv[c] = sp[c * br->cs];
+        z0[c] = (prm.rk == 1 || prm.rk == 2) ? P[o + c * pcs] : make_float2(0.f, 0.f);
+        a0[c] = prm.rk >= 2 ? br->acc[o + c * pcs] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float2 nv;
+        const float2 ra = rk_core_r<N, DIM, false>(row, mid, kh, ik2, c, pv[c], sv[c], a0[c], z0[c], prm, fscale, nv);
+        if (prm.rk == 0) P[o + c * pcs] = sv[c];
+        if (prm.rk == 1 || prm.rk == 2) br->acc[o + c * pcs] = ra;
+        sp[c * br->cs] = nv;
+        if (prm.rk == 3) bad |= !isfinite(nv.x + nv.y);
+      }
+    }
+  }
+  if constexpr (FUSED) {
+    if (bad) atomicOr(br->err, kErrNonFinite);
+  }
+}
+
+// FUSED: the band-fused RK step (BandRk; the constant-power coefficient then comes from
+// the stage's x inverse, band_kf = 0 here).
+template <int N, int DIM, bool FUSED = false>
+__global__ void __launch_bounds__(TW * Fft<N>::T)
+kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
+            const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
+            double inv_n2d, double eps_inj, double* __restrict__ band_scale, const BandRk br = BandRk{}) {
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
+  constexpr int NMID = DIM == 3 ? N : 1;
+  __shared__ float2 sm[xpad_len<TW>(N) * TW];
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
+  const int km = DIM == 3 ? kmb - kd : 0;
+  const int mid = km < 0 ? km + N : km;
+  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
+  const int batch = blockIdx.z;
+  const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
+  if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
+    band_coefficient<DIM>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30,
+                          band_scale + batch);
+  float2 d[3][E];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
+  kx_fwd_band_tile<N, DIM, FUSED>(d, t, kh, kmb, kd, kt, sm + p, P, pcs, bp, tw, &br, batch);
+}
+
+// Persistent 3D variant of kx_fwd_band: tiles (column tile, band row kmb) are walked
+// blockIdx.x, + gridDim.x, ...; the next tile's DU block (TW columns x N x rows x 3
+// components at middle row `mid`) arrives by one 4D bulk tensor load while the current
+// one is transformed. dmap: DU as (kt, N mid, N x, 3 * batch), box (TW, 1, min(N, 256), 3).
+template <int N, bool FUSED = false>
+__global__ void __launch_bounds__(TW * Fft<N>::T, TW * Fft<N>::T >= 512 ? 1 : 2)
+kx_fwd_band_tma(const __grid_constant__ CUtensorMap dmap, int kt, int kd, float2* __restrict__ P, long long pcs,
+                const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
+                double inv_n2d, double eps_inj, double* __restrict__ band_scale, int* __restrict__ err,
+                const __grid_constant__ BandRk br) {
+  using K = KxTma<N>;
+  constexpr int E = Fft<N>::E, T = Fft<N>::T;
+  extern __shared__ __align__(128) float2 s_dyn[];
+  float2* stage = s_dyn;
+  float2* sm = s_dyn + K::STAGE;
+  __shared__ uint64_t bar;
+  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  const int batch = blockIdx.y;
+  const int ntx = kt / TW, nb = 2 * kd + 1, ntiles = ntx * nb;
+  if (band_kf > 0 && blockIdx.x == 0)
+    band_coefficient<3>(us + (long long)batch * 3 * cs, cs, N, band_kf, inv_n2d, eps_inj, 1e-30, band_scale + batch);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int tile) {
+    const int kmb = tile / ntx, x0 = (tile % ntx) * TW;
+    const int km = kmb - kd, mid = km < 0 ? km + N : km;
+    mbar_arrive_expect_tx(&bar, K::BYTES);
+#pragma unroll
+    for (int l = 0; l < K::LOADS; ++l)
+      tma_load_4d(stage + l * 3 * K::NY * TW, &dmap, &bar, x0, mid, l * K::NY, 3 * batch);
+  };
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile);
+  unsigned parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool got = threadIdx.x < 32 ? mbar_wait(&bar, parity) : true;  // as in kx_inv_tma
+    if (__syncthreads_or(!got)) {
+      if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+      mbar_wait(&bar, parity);
+      return;
+    }
+    if (threadIdx.x >= 32) mbar_wait(&bar, parity);
+    parity ^= 1u;
+    float2 d[3][E];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int row = t + T * e;
+        d[c][e] = stage[(((row / K::NY) * 3 + c) * K::NY + row % K::NY) * TW + p];
+      }
+    __syncthreads();
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && next < ntiles) {
+      fence_proxy_async_smem();
+      issue(next);
+    }
+    kx_fwd_band_tile<N, 3, FUSED>(d, t, (tile % ntx) * TW + p, tile / ntx, kd, kt, sm + p, P, pcs,
+                                  (long long)batch * 3 * pcs, tw, &br, batch);
+  }
+}
+
+// ------------------------------------------------------------------------------
+// Elementwise linear terms + RK4 stage combination (spectral_solver.py:59, :74-80),
+// two complex values (one float4) per thread over all 3 components:
+//   du = P(k) (kept band, else 0) - nu k^2 us [- drag us + forcing terms]
+//   rk 0   : out <- us + b dt du                               (us = u0; no acc)
+//   rk 1   : acc <- u0 + (a0/b0)(us - u0) + a dt du, out <- u0 + b dt du
+//   rk 2   : acc += a dt du,       out <- u0 + b dt du         (us aliases out)
+//   rk 3   : fin <- acc + a dt du
+//   rk -1  : out <- du (the reference's rhs_fn)
+// Every thread loads all its operands before storing (us/out and acc alias).
+// VIF: the integrating-factor form (a separate instantiation, so the reference's explicit
+// form keeps its own code).
+// ------------------------------------------------------------------------------
+// rk_core: one mode given its indices (kxi, mid, kh: storage indices on the x, middle
+// and half axes; kx, km: their signed wavenumbers); rk_elem: by flat index i.
+template <int N, int DIM, bool VIF = false>
+__device__ __forceinline__ float2 rk_core(int kxi, int mid, int kh, int kx, int km, int c, float2 sv, float2 a0,
+                                          float2 z0, const float2* __restrict__ P, long long pcs, int kt, int kd,
+                                          const EpiParams& prm, float fscale, float2& nv) {
+  const int ik2 = kx * kx + km * km + kh * kh;
+  float2 r = make_float2(0.f, 0.f);
+  // band rows as unsigned offsets: in the band iff 0 <= k + kd <= 2 kd on every axis
+  const unsigned nb = 2u * (unsigned)kd + 1u;
+  const unsigned bx = (unsigned)(kx + kd);
+  const unsigned bm = DIM == 3 ? (unsigned)(km + kd) : 0u;
+  if (bx < nb && bm < nb && (unsigned)kh <= (unsigned)kd) {
+    const long long row = DIM == 3 ? (long long)bx * nb + bm : (long long)bx;
+    r = __ldg(P + c * pcs + row * kt + kh);
+  }
+  return rk_core_r<N, DIM, VIF>(kxi, mid, kh, ik2, c, r, sv, a0, z0, prm, fscale, nv);
 }
 
 template <int N, int DIM, bool VIF = false>
@@ -1462,15 +1620,7 @@ k_rk_update_lin(const float2* __restrict__ P, long long pcs, int kt, int kd, con
                                     nv[h]);
     } else {
       const float z = (prm.nu * (float)(kx * kx + km * km + kh[h] * kh[h]) + prm.drag) * prm.dt;
-      float f;
-      if (prm.rk == 0)
-        f = fmaf(-0.5f, z, 1.f);
-      else if (prm.rk == 1)
-        f = fmaf(z, fmaf(0.25f, z, -0.5f), 1.f);
-      else if (prm.rk == 2)
-        f = fmaf(z, fmaf(z, fmaf(-0.25f, z, 0.5f), -1.f), 1.f);
-      else
-        f = fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.f / 24.f, -1.f / 6.f), 0.5f), -1.f), 1.f);
+      const float f = lin_stage_factor(prm.rk, z);
       nv[h] = make_float2(f * z0.x, f * z0.y);
     }
   }

@@ -22,6 +22,8 @@ struct DnsOps {
 
   static inline int tma_band_ctas = 0;
   static inline int tma_plain_ctas = 0;  // x inverse without curl (irfftn)
+  static inline int tma_lin_ctas = 0;    // band-fused RK step: x inverse and band pass
+  static inline int tma_band_fused_ctas = 0;
 
   // resident CTAs (all SMs) of a persistent kernel with K::SMEM dynamic shared memory
   template <typename F>
@@ -49,6 +51,8 @@ struct DnsOps {
       tma_ctas = persistent_ctas(kx_inv_tma<N, true, true>);
       tma_band_ctas = persistent_ctas(kx_fwd_band_tma<N>);
       tma_plain_ctas = persistent_ctas(kx_inv_tma<N, false>);
+      tma_lin_ctas = persistent_ctas(kx_inv_tma<N, true, true, true>);
+      tma_band_fused_ctas = persistent_ctas(kx_fwd_band_tma<N, true>);
     }
   }
 
@@ -74,27 +78,38 @@ struct DnsOps {
       L3ES_LAUNCH(c, KK_Y_INV, bytes, s, ky_inv_rhs<N, 0><<<g, KY::THREADS, 0, s>>>(c.W, c.Wx, c.fs, c.tw));
   }
 
-  // x inverse pass with curl prologue: us -> W (6 fields)
+  // x inverse pass with curl prologue: us -> W (6 fields); xl: the x inverse of a
+  // band-fused RK stage (us is then the state xl->S)
   template <int DIM>
-  static void x_inverse(const Ctx& c, const float2* us, double bytes, cudaStream_t s) {
+  static void x_inverse(const Ctx& c, const float2* us, double bytes, cudaStream_t s, const XLin* xl = nullptr) {
     const long long mc = c.nmid * H;
     if constexpr (DIM == 3 && N >= 64) {
       CUtensorMap map;
       const unsigned long long dims[3] = {(unsigned long long)mc, N, 3ull * c.batch};
       const unsigned long long strides[2] = {8ull * mc, 8ull * c.cs};
       const unsigned box[3] = {TW, KxTma<N>::NY, 3};
-      if (c.sched.x_bulk && tma_ctas > 0 && tma_encode(&map, us, 3, dims, strides, box)) {
+      const int ctas = xl ? tma_lin_ctas : tma_ctas;
+      if (c.sched.x_bulk && ctas > 0 && tma_encode(&map, us, 3, dims, strides, box)) {
         const int ntiles = (int)(mc / TW);
-        const int gx = std::max(1, std::min(ntiles, tma_ctas / c.batch));
-        L3ES_LAUNCH(c, KK_X_INV, bytes, s,
-                    kx_inv_tma<N, true, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
-                        map, c.W, c.fs, c.tw, ntiles, c.err, c.Wx));
+        const int gx = std::max(1, std::min(ntiles, ctas / c.batch));
+        if (xl)
+          L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                      kx_inv_tma<N, true, true, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
+                          map, c.W, c.fs, c.tw, ntiles, c.err, c.Wx, *xl));
+        else
+          L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                      kx_inv_tma<N, true, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
+                          map, c.W, c.fs, c.tw, ntiles, c.err, c.Wx, XLin{}));
         return;
       }
     }
-    L3ES_LAUNCH(c, KK_X_INV, bytes, s,
-                kx_inv<N, DIM, true, DIM == 3><<<dim3((unsigned)((mc + TW - 1) / TW), c.batch), TX, 0, s>>>(
-                    us, c.cs, c.W, c.fs, c.tw, c.Wx));
+    const dim3 g((unsigned)((mc + TW - 1) / TW), c.batch);
+    if (xl)
+      L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                  kx_inv<N, DIM, true, DIM == 3, true><<<g, TX, 0, s>>>(us, c.cs, c.W, c.fs, c.tw, c.Wx, *xl, c.err));
+    else
+      L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                  kx_inv<N, DIM, true, DIM == 3><<<g, TX, 0, s>>>(us, c.cs, c.W, c.fs, c.tw, c.Wx));
   }
 
   // us: field the RHS is evaluated on; S: state; out: RK stage field (or du for rk=-1)
@@ -107,9 +122,30 @@ struct DnsOps {
     const double B = c.batch, A = 8.0 * 3.0 * c.cs * B;  // bytes of one 3-component spectrum
     const double Adu = 8.0 * 3.0 * c.ds * B;               // bytes of the truncated DU field
     const double rows = DIM == 3 ? (2.0 * c.kd + 1.0) / N : 1.0;  // kept y rows
+    const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
+    // band-fused RK step (XLin): us == S; fb = the band's share of the modes
+    const bool fused = prm.band_rk && rk >= 0;
+    const double fb = (double)c.pcs / (double)c.cs;
+    XLin xl{};
+    if (fused) {
+      xl.S = S;
+      xl.cs = c.cs;
+      xl.nu_b = c.nu_b;
+      xl.drag = prm.drag;
+      xl.dt = prm.dt;
+      xl.kd = c.kd;
+      xl.kt = c.kt;
+      xl.rk = rk;
+      xl.band_kf = prm.band_kf2 > 0 ? c.kf : 0;
+      xl.inv_n2d = inv_n2d;
+      xl.eps_inj = c.eps_inj;
+      xl.band_scale = c.band;
+    }
     // 3D: the x pass stores u_x, curl_y, curl_z in W and u_y, u_z in the side buffer
-    // Wx (curl_x is not stored); the y pass writes all six fields of W
-    x_inverse<DIM>(c, us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A, s);
+    // Wx (curl_x is not stored); the y pass writes all six fields of W. The last
+    // band-fused stage also writes the new state outside the band.
+    x_inverse<DIM>(c, us, (DIM == 3 ? 8.0 : 9.0) / 3.0 * A + (fused && rk == 3 ? (1.0 - fb) * A : 0.0), s,
+                   fused ? &xl : nullptr);
     if (DIM == 3) y_inv_rhs(c, 11.0 / 3.0 * A, s);
     bool line_done = false;
     if constexpr (N >= 64 && N <= 256) {  // two real lines per complex FFT, persistent
@@ -149,8 +185,33 @@ struct DnsOps {
     // band x-FFT + projection into P, then the elementwise RK update
     const int nb = 2 * c.kd + 1;
     const double Ap = 8.0 * 3.0 * c.pcs * B;
+    if (fused) {
+      // the stage combination on the band: rk 0 reads S and writes P (= u0) and S; rk 1
+      // reads S, P and writes acc, S; rk 2 reads S, P, acc and writes acc, S; rk 3 reads
+      // S, acc and writes S
+      const BandRk br{S, c.C, c.cs, prm, c.band, c.nu_b, c.err};
+      const double bb = Adu * rows + Ap * (rk == 0 ? 3.0 : rk == 1 ? 4.0 : rk == 2 ? 5.0 : 3.0);
+      if constexpr (DIM == 3 && N >= 64) {
+        const bool bulk = c.sched.band_bulk < 0 ? N >= 256 : c.sched.band_bulk != 0;
+        CUtensorMap map;
+        const unsigned long long dims[4] = {(unsigned long long)c.kt, N, N, 3ull * c.batch};
+        const unsigned long long strides[3] = {8ull * c.kt, 8ull * N * c.kt, 8ull * c.ds};
+        const unsigned box[4] = {TW, 1, KxTma<N>::NY, 3};
+        if (bulk && tma_band_fused_ctas > 0 && tma_encode(&map, c.DU, 4, dims, strides, box)) {
+          const int ntiles = (c.kt / TW) * nb;
+          const int gx = std::max(1, std::min(ntiles, tma_band_fused_ctas / c.batch));
+          L3ES_LAUNCH(c, KK_X_EPI, bb, s,
+                      kx_fwd_band_tma<N, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
+                          map, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, 0, inv_n2d, c.eps_inj, c.band, c.err, br));
+          return;
+        }
+      }
+      L3ES_LAUNCH(c, KK_X_EPI, bb, s,
+                  kx_fwd_band<N, DIM, true><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
+                      c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, 0, inv_n2d, c.eps_inj, c.band, br));
+      return;
+    }
     // (block 0 of each trajectory also computes the constant-power coefficient of us)
-    const double inv_n2d = 1.0 / (DIM == 3 ? std::pow((double)N, 6) : std::pow((double)N, 4));
     bool band_done = false;
     // by default from 256^3: smaller grids have too few band tiles per persistent CTA to
     // pipeline (measured at 128^3: 9.5 us persistent vs 8.4 us one-shot)
@@ -166,7 +227,7 @@ struct DnsOps {
         L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
                     kx_fwd_band_tma<N><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
                         map, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
-                        c.eps_inj, c.band, c.err));
+                        c.eps_inj, c.band, c.err, BandRk{}));
         band_done = true;
       }
     }
@@ -223,7 +284,7 @@ struct DnsOps {
         const int gx = std::max(1, std::min(ntiles, tma_plain_ctas / c.batch));
         L3ES_LAUNCH(c, KK_X_INV_PLAIN, 2.0 * A, s,
                     kx_inv_tma<N, false><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(map, c.W, c.fs, c.tw, ntiles,
-                                                                                        c.err, nullptr));
+                                                                                        c.err, nullptr, XLin{}));
         x_done = true;
       }
     }

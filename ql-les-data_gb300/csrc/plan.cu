@@ -417,6 +417,19 @@ int l3es_plan_set_schedule(l3es_plan* plan, const int32_t* sched4) {
   return L3ES_OK;
 }
 
+int l3es_plan_get_step_form(const l3es_plan* plan, int32_t* form) {
+  if (!plan || !form) return fail(L3ES_EINVAL, "l3es_plan_get_step_form: null argument");
+  *form = plan->ctx.step_form;
+  return L3ES_OK;
+}
+
+int l3es_plan_set_step_form(l3es_plan* plan, int32_t form) {
+  if (!plan) return fail(L3ES_EINVAL, "l3es_plan_set_step_form: null plan");
+  if (form < 0 || form > 2) return fail(L3ES_EINVAL, "l3es_plan_set_step_form: form is 0, 1 or 2");
+  plan->ctx.step_form = form;
+  return L3ES_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------
@@ -577,8 +590,12 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
   // closed-form stages outside the stage region (k_rk_update): explicit scheme, forcing
   // terms inside the region (band forcing |k| <= kf, Kolmogorov mode kh = kolm_k)
   const int kf_band = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf : 0;
-  const int lin_ok = c.lin_enabled && d.scheme != L3ES_SCHEME_INTEGRATING_FACTOR && kf_band <= c.kd &&
+  const int lin_ok = c.step_form >= 1 && d.scheme != L3ES_SCHEME_INTEGRATING_FACTOR && kf_band <= c.kd &&
                      kf_band < c.kt && (d.kolm_k <= 0 || d.kolm_k < c.kt);
+  // the band-fused form: the band pass combines the stages on the band in place in S,
+  // the x inverse applies the closed form to every other mode; its accumulator lives in
+  // C in the band's compact layout (kt <= N/2 + 1, i.e. N >= 16, keeps that inside C)
+  const int band_rk = lin_ok && c.step_form >= 2 && c.kt <= c.h;
   for (int st = 0; st < nsteps; ++st) {
     for (int rk = 0; rk < 4; ++rk) {
       EpiParams prm;
@@ -593,7 +610,11 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
       prm.if_h = d.scheme == L3ES_SCHEME_INTEGRATING_FACTOR ? (float)d.dt : 0.f;
       prm.dt = (float)d.dt;
       prm.lin = lin_ok;
-      plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
+      prm.band_rk = band_rk;
+      if (band_rk)
+        plan->tab.stage(c, S, S, S, rk, prm, s);
+      else
+        plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
     }
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
     double* ke_final = (ke_dev && st == nsteps - 1) ? ke_dev : nullptr;

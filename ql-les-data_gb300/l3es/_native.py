@@ -30,6 +30,8 @@ _SIGNATURES = {
     "l3es_plan_set_nu": (ctypes.c_int, [_P, _P, _I]),
     "l3es_plan_get_schedule": (ctypes.c_int, [_P, _P]),
     "l3es_plan_set_schedule": (ctypes.c_int, [_P, _P]),
+    "l3es_plan_get_step_form": (ctypes.c_int, [_P, _P]),
+    "l3es_plan_set_step_form": (ctypes.c_int, [_P, ctypes.c_int32]),
     "l3es_plan_autotune": (ctypes.c_int, [_P, ctypes.c_char_p, _P]),
     "l3es_graph_begin": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "l3es_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
@@ -330,6 +332,22 @@ class Plan:
         cur.update(sched)
         v = (ctypes.c_int32 * 4)(*[int(cur[k]) for k in self.SCHEDULE_KEYS])
         _check(self._lib.l3es_plan_set_schedule(self._h, v), "l3es_plan_set_schedule")
+
+    STEP_FORMS = ("whole_spectrum", "closed_form_outside_rows", "band_fused")
+
+    @property
+    def step_form(self) -> int:
+        """Form of the explicit RK4 step (l3es_plan_get_step_form): 0 one elementwise
+        update of the whole spectrum per stage, 1 the closed form of the linear decay
+        outside the dealiased rows, 2 (default) the stage combination fused into the band
+        pass. All forms compute the reference's RK4 step."""
+        v = ctypes.c_int32()
+        _check(self._lib.l3es_plan_get_step_form(self._h, ctypes.byref(v)), "l3es_plan_get_step_form")
+        return int(v.value)
+
+    @step_form.setter
+    def step_form(self, form: int) -> None:
+        _check(self._lib.l3es_plan_set_step_form(self._h, int(form)), "l3es_plan_set_step_form")
 
     def autotune(self, cache_path=None, stream=None) -> dict:
         """Pick the fastest kernel schedule for this plan (l3es_plan_autotune); cache_path

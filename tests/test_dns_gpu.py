@@ -508,6 +508,49 @@ def test_every_kernel_schedule_gives_the_same_step(n):
         assert _rel(g.cpu().numpy(), ref) < 2e-6, combo
 
 
+@pytest.mark.parametrize("case", ["3d64_const_power", "3d128_none", "3d64_const_power_batch3_x_plain",
+                                  "2d256_kolmogorov", "3d256_const_power"])
+def test_rk_step_forms_agree(case):
+    """The three forms of the explicit RK4 step (one elementwise update of the whole
+    spectrum; the closed form of the linear decay outside the dealiased rows; the stage
+    combination fused into the band pass with every other mode scaled inside the next
+    x inverse) compute the same steps to FP32 rounding, with the one-tile and the
+    persistent x and band passes, single and batched plans."""
+    steps = 3
+    if case.startswith("2d"):
+        n = 256
+        u = R.init_u_random2d(n, 11)
+        uh0 = np.fft.rfftn(u, axes=(1, 2)).squeeze()[None]
+        kw = dict(dim=2, n=n, nu=1e-3, dt=1e-3, drag=0.1, kolm_k=4, kolm_amp=1.0)
+        batch = 1
+    else:
+        n = int(case[2:case.index("_")])
+        batch = 3 if "batch3" in case else 1
+        uh0 = []
+        for b in range(batch):
+            u = R.init_u_hit(n, 3 + b, spectrum="k4exp", kp=3.0)
+            uh0.append(np.fft.rfftn(u * np.sqrt(0.5 / R.kinetic_energy(u)), axes=(1, 2, 3)))
+        uh0 = np.stack(uh0)
+        kw = dict(dim=3, n=n, nu=5e-3, dt=2e-3)
+        if "const_power" in case:
+            kw.update(forcing="const_power", kf=2, eps_inj=0.1)
+    p = _plan(batch=batch, **kw)
+    assert p.step_form == 2
+    if "x_plain" in case:
+        p.set_schedule({"x_bulk": 0, "band_bulk": 0})
+    outs = {}
+    for form in (0, 1, 2):
+        p.step_form = form
+        g = _c64(uh0 if batch > 1 else uh0[0])
+        p.step(g, steps)
+        p.check()
+        outs[form] = g.cpu().numpy()
+    assert _rel(outs[1], outs[0]) < 2e-6
+    assert _rel(outs[2], outs[0]) < 2e-6
+    with pytest.raises(Exception, match="form"):
+        p.step_form = 3
+
+
 def test_line_pass_variants_agree_in_2d_at_256():
     """2D Kolmogorov flow at 256^2 (drag, sin 4y forcing): every line pass variant gives
     the same steps, and the radix-16 forms against the FP64 oracle."""
