@@ -1354,20 +1354,14 @@ __device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int 
     block_fft<N, E, kFwd, TW>(d[c], sm, t, tw, 1);
     __syncthreads();
   }
-  EpiParams prm;
-  float fscale = 0.f;
-  if constexpr (FUSED) {
-    prm = br->prm;
-    prm.nu = br->nu_b[batch];
-    fscale = prm.band_kf2 > 0 ? (float)br->band_scale[batch] : 0.f;
-  }
-  bool bad = false;
   // (kt can exceed the half axis only at N = 8: those columns hold no mode of S)
   const bool live = !FUSED || kh < H;
+  bool inb[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int kx = kfull(t + T * e, N);
-    if ((unsigned)(kx + kd) > 2u * (unsigned)kd || !live) continue;  // |kx| > kd
+    inb[e] = live && (unsigned)(kx + kd) <= 2u * (unsigned)kd;  // |kx| <= kd
+    if (!inb[e]) continue;
     float k0, k1, k2;
     kvec<DIM>(kx, km, kh, k0, k1, k2);
     const bool keep = kh <= kd;
@@ -1378,36 +1372,66 @@ __device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int 
     const float2 v2 = keep ? d[2][e] : make_float2(0.f, 0.f);
     const float pr = (v0.x * k0 + v1.x * k1 + v2.x * k2) * inv;
     const float pi_ = (v0.y * k0 + v1.y * k1 + v2.y * k2) * inv;
-    const long long o = bp + ((long long)(kx + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
-    const float2 pv[3] = {make_float2(v0.x - pr * k0, v0.y - pi_ * k0), make_float2(v1.x - pr * k1, v1.y - pi_ * k1),
-                          make_float2(v2.x - pr * k2, v2.y - pi_ * k2)};
+    d[0][e] = make_float2(v0.x - pr * k0, v0.y - pi_ * k0);
+    d[1][e] = make_float2(v1.x - pr * k1, v1.y - pi_ * k1);
+    d[2][e] = make_float2(v2.x - pr * k2, v2.y - pi_ * k2);
     if constexpr (!FUSED) {
+      const long long o = bp + ((long long)(kx + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) P[o + c * pcs] = pv[c];
-    } else {
-      // the stage combination of rk_core on this band mode, in place in S; P holds the
-      // step's initial band values (written at rk 0), br->acc the accumulator
-      const int row = t + T * e;
-      float2* sp = br->S + (long long)batch * 3 * br->cs + ((long long)row * NMID + mid) * H + kh;
-      float2 sv[3], z0[3], a0[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        sv[c] = sp[c * br->cs];
-        z0[c] = (prm.rk == 1 || prm.rk == 2) ? P[o + c * pcs] : make_float2(0.f, 0.f);
-        a0[c] = prm.rk >= 2 ? br->acc[o + c * pcs] : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float2 nv;
-        const float2 ra = rk_core_r<N, DIM, false>(row, mid, kh, ik2, c, pv[c], sv[c], a0[c], z0[c], prm, fscale, nv);
-        if (prm.rk == 0) P[o + c * pcs] = sv[c];
-        if (prm.rk == 1 || prm.rk == 2) br->acc[o + c * pcs] = ra;
-        sp[c * br->cs] = nv;
-        if (prm.rk == 3) bad |= !isfinite(nv.x + nv.y);
-      }
+      for (int c = 0; c < 3; ++c) P[o + c * pcs] = d[c][e];
     }
   }
   if constexpr (FUSED) {
+    // the stage combination of rk_core on the band modes, in place in S; P holds the
+    // step's initial band values (written at rk 0), br->acc the accumulator. Software
+    // pipelined by one mode: the next mode's operands are loaded before this mode's
+    // results are stored (a load may not pass an earlier store to the same arrays, so
+    // load/store pairs in program order would each wait on memory).
+    EpiParams prm = br->prm;
+    prm.nu = br->nu_b[batch];
+    const float fscale = prm.band_kf2 > 0 ? (float)br->band_scale[batch] : 0.f;
+    float2* sb = br->S + (long long)batch * 3 * br->cs + (long long)mid * H + kh;
+    auto sofs = [&](int e) { return (long long)(t + T * e) * NMID * H; };
+    auto pofs = [&](int e) {
+      return bp + ((long long)(kfull(t + T * e, N) + kd) * (DIM == 3 ? nb : 1) + kmb) * kt + kh;
+    };
+    float2 sv[3], z0[3], a0[3], sv1[3], z01[3], a01[3];
+    auto load = [&](int e, float2(&s_)[3], float2(&z_)[3], float2(&a_)[3]) {
+      const long long so = sofs(e), o = pofs(e);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        s_[c] = sb[so + c * br->cs];
+        z_[c] = (prm.rk == 1 || prm.rk == 2) ? P[o + c * pcs] : make_float2(0.f, 0.f);
+        a_[c] = prm.rk >= 2 ? br->acc[o + c * pcs] : make_float2(0.f, 0.f);
+      }
+    };
+    if (inb[0]) load(0, sv, z0, a0);
+    bool bad = false;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (e + 1 < E && inb[e + 1]) load(e + 1, sv1, z01, a01);
+      if (inb[e]) {
+        const int row = t + T * e;
+        const int kx = kfull(row, N);
+        const long long so = sofs(e), o = pofs(e);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float2 nv;
+          const float2 ra = rk_core_r<N, DIM, false>(row, mid, kh, kx * kx + km * km + kh * kh, c, d[c][e], sv[c],
+                                                     a0[c], z0[c], prm, fscale, nv);
+          if (prm.rk == 0) P[o + c * pcs] = sv[c];
+          if (prm.rk == 1 || prm.rk == 2) br->acc[o + c * pcs] = ra;
+          sb[so + c * br->cs] = nv;
+          if (prm.rk == 3) bad |= !isfinite(nv.x + nv.y);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sv[c] = sv1[c];
+        z0[c] = z01[c];
+        a0[c] = a01[c];
+      }
+    }
     if (bad) atomicOr(br->err, kErrNonFinite);
   }
 }
