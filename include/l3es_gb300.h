@@ -117,20 +117,22 @@ int l3es_plan_set_schedule(l3es_plan* plan, const int32_t* sched4);
  *   0 one elementwise update of the whole spectrum per stage,
  *   1 the same, with modes outside the dealiased rows taking the closed form of their
  *     linear decay (no nonlinear or forcing term reaches them),
- *   2 (default) the stage combination fused into the band x pass, in place on the
- *     band, and every other mode scaled by its closed form inside the next stage's
- *     x inverse (no elementwise pass).
+ *   2 the stage combination fused into the band x pass, in place on the band, and
+ *     every other mode scaled by its closed form inside the next stage's x inverse (no
+ *     elementwise pass).
+ * Plans start with form 2 in 3D and form 1 in 2D (the 2D band pass has too few CTAs to
+ * hide the fused epilogue's memory latency).
  * Forms 1 and 2 apply when the forcing lies inside the band (constant-power kf <= kd,
  * Kolmogorov wavenumber < kt); otherwise, and for the integrating-factor scheme, the
  * step takes form 0. */
 int l3es_plan_get_step_form(const l3es_plan* plan, int32_t* form);
 int l3es_plan_set_step_form(l3es_plan* plan, int32_t form);
 
-/* Autotuner: times the plan's right-hand side on its own scratch under each schedule
- * choice (one knob at a time) and keeps the fastest. cache_path (nullable) names a
- * text file of earlier results, one line per GPU model, dim, N and batch; a hit skips
- * the timing, a miss appends the result. Synchronises the stream; not while recording
- * a graph. */
+/* Autotuner: times one RK4 step of the plan (its step form, on its own scratch) under
+ * each schedule choice (one knob at a time) and keeps the fastest. cache_path
+ * (nullable) names a text file of earlier results, one line per GPU model, dim, N,
+ * batch and step form; a hit skips the timing, a miss appends the result.
+ * Synchronises the stream; not while recording a graph. */
 int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void* stream);
 
 /* Diagnostics of the drivers, FP64 results on the device (per trajectory):

@@ -157,7 +157,8 @@ struct Ctx {
   int* err = nullptr;          // device error word: nonzero after a kernel wait timed out
   int step_form = 2;           // explicit RK4 step (run_steps): 0 per-mode update of the whole
                                // spectrum, 1 closed-form stages outside the stage region, 2 the
-                               // stage combination fused into the band pass (l3es_plan_set_step_form)
+                               // stage combination fused into the band pass (l3es_plan_set_step_form;
+                               // plans start at 2 in 3D, 1 in 2D)
   Schedule sched;              // kernel variants of the step
   int kf = 0;                  // forcing band 0 < |k|^2 <= kf^2
   double eps_inj = 0.0;        // constant-power injection rate

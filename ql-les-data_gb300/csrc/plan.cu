@@ -237,6 +237,10 @@ int l3es_plan_create(const l3es_plan_desc* desc, l3es_plan** out) {
   c.kd = dealias_kd(n);
   c.kt = ((c.kd + 1 + TW - 1) / TW) * TW;
   if (n == 256) c.sched.line_pair = 3;  // the staged radix-16 line pass (measured best at 256)
+  // the band-fused step in 3D; a 2D band pass has one CTA per 8 half-axis columns (11 at
+  // 256^2), too few to hide its epilogue's loads (2D Kolmogorov 256^2 with particles:
+  // 104.5 us per step fused, 101.4 us with the elementwise update)
+  c.step_form = dim == 3 ? 2 : 1;
   c.nmid = dim == 3 ? n : 1;
   c.cs = c.nmid * n * c.h;
   c.fs = c.cs;
@@ -446,7 +450,8 @@ static std::string tune_key(const l3es_plan* p) {
   for (char& ch : name)
     if (ch == ' ') ch = '_';
   return name + "|sm" + std::to_string(prop.major) + std::to_string(prop.minor) + "|d" + std::to_string(p->ctx.dim) +
-         "|n" + std::to_string(p->ctx.n) + "|b" + std::to_string(p->ctx.batch);
+         "|n" + std::to_string(p->ctx.n) + "|b" + std::to_string(p->ctx.batch) + "|f" +
+         std::to_string(p->ctx.step_form);
 }
 
 static bool tune_cache_read(const char* path, const std::string& key, int32_t* v) {
@@ -489,21 +494,52 @@ static void tune_cache_write(const char* path, const std::string& key, const int
   std::fclose(f);
 }
 
-// mean milliseconds of one right-hand side with the plan's current schedule
-static float time_rhs(l3es_plan* p, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+// The four stages of one RK4 step of the state S in the plan's step form
+// (spectral_solver.py:65-80; the forcing rescale of ekin_tot follows in run_steps).
+static void rk4_stages(l3es_plan* plan, float2* S, cudaStream_t s) {
+  const Ctx& c = plan->ctx;
+  const l3es_plan_desc& d = plan->desc;
+  static const double a_rk4[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+  static const double b_rk4[3] = {0.5, 0.5, 1.0};
+  // closed-form stages outside the stage region (k_rk_update): explicit scheme, forcing
+  // terms inside the region (band forcing |k| <= kf, Kolmogorov mode kh = kolm_k)
+  const int kf_band = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf : 0;
+  const int lin_ok = c.step_form >= 1 && d.scheme != L3ES_SCHEME_INTEGRATING_FACTOR && kf_band <= c.kd &&
+                     kf_band < c.kt && (d.kolm_k <= 0 || d.kolm_k < c.kt);
+  // the band-fused form: the band pass combines the stages on the band in place in S,
+  // the x inverse applies the closed form to every other mode; its accumulator lives in
+  // C in the band's compact layout (kt <= N/2 + 1, i.e. N >= 16, keeps that inside C)
+  const int band_rk = lin_ok && c.step_form >= 2 && c.kt <= c.h;
+  for (int rk = 0; rk < 4; ++rk) {
+    EpiParams prm;
+    prm.a_dt = (float)(a_rk4[rk] * d.dt);
+    prm.b_dt = rk < 3 ? (float)(b_rk4[rk] * d.dt) : 0.f;
+    prm.nu = (float)d.nu;
+    prm.drag = (float)d.drag;
+    prm.kolm_amp = (float)d.kolm_amp;
+    prm.kolm_k = d.kolm_k;
+    prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
+    prm.rk = rk;
+    prm.if_h = d.scheme == L3ES_SCHEME_INTEGRATING_FACTOR ? (float)d.dt : 0.f;
+    prm.dt = (float)d.dt;
+    prm.lin = lin_ok;
+    prm.band_rk = band_rk;
+    if (band_rk)
+      plan->tab.stage(c, S, S, S, rk, prm, s);
+    else
+      plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
+  }
+}
+
+// mean milliseconds of one RK4 step in the plan's step form with its current schedule,
+// on the zeroed stage scratch T as the state (timing only: the explicit forms then alias
+// their stage field with the state; zeros stay finite through every term)
+static float time_step(l3es_plan* p, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
   const Ctx& c = p->ctx;
-  const l3es_plan_desc& d = p->desc;
-  EpiParams prm{};
-  prm.nu = (float)d.nu;
-  prm.drag = (float)d.drag;
-  prm.kolm_amp = (float)d.kolm_amp;
-  prm.kolm_k = d.kolm_k;
-  prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
-  prm.rk = -1;
-  for (int i = 0; i < 2; ++i) p->tab.stage(c, c.Tb, nullptr, c.C, -1, prm, s);
-  const int reps = c.cs * c.batch > (1 << 20) ? 5 : 20;
+  rk4_stages(p, c.Tb, s);
+  const int reps = c.cs * c.batch > (1 << 20) ? 2 : 5;
   cudaEventRecord(e0, s);
-  for (int i = 0; i < reps; ++i) p->tab.stage(c, c.Tb, nullptr, c.C, -1, prm, s);
+  for (int i = 0; i < reps; ++i) rk4_stages(p, c.Tb, s);
   cudaEventRecord(e1, s);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -536,7 +572,7 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
     const bool knob[4] = {c.dim == 3 && n >= 64, c.dim == 3 && n >= 128, n >= 64 && n <= 256,
                           c.dim == 3 && n >= 64};
     const int nval[4] = {2, 2, n == 256 ? 4 : 2, 2};  // the line pass has two radix-16 forms at 256
-    float best = time_rhs(plan, s, e0, e1);
+    float best = time_step(plan, s, e0, e1);
     for (int k = 0; k < 4; ++k) {
       if (!knob[k]) continue;
       const int keep = v[k];
@@ -545,7 +581,7 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
         if (val == keep) continue;
         v[k] = val;
         l3es_plan_set_schedule(plan, v);
-        const float t = time_rhs(plan, s, e0, e1);
+        const float t = time_step(plan, s, e0, e1);
         if (t < best) {
           best = t;
           pick = val;
@@ -583,39 +619,10 @@ static int run_steps(l3es_plan* plan, void* u_hat, float* u_out, int32_t nsteps,
   const Ctx& c = plan->ctx;
   const l3es_plan_desc& d = plan->desc;
   float2* S = (float2*)u_hat;
-  static const double a_rk4[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
-  static const double b_rk4[3] = {0.5, 0.5, 1.0};
   const double inv_n2d = 1.0 / std::pow((double)c.n, 2 * c.dim);
   const double eps64 = 2.220446049250313e-16;  // jnp.finfo(float).eps, spectral_solver.py:23
-  // closed-form stages outside the stage region (k_rk_update): explicit scheme, forcing
-  // terms inside the region (band forcing |k| <= kf, Kolmogorov mode kh = kolm_k)
-  const int kf_band = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf : 0;
-  const int lin_ok = c.step_form >= 1 && d.scheme != L3ES_SCHEME_INTEGRATING_FACTOR && kf_band <= c.kd &&
-                     kf_band < c.kt && (d.kolm_k <= 0 || d.kolm_k < c.kt);
-  // the band-fused form: the band pass combines the stages on the band in place in S,
-  // the x inverse applies the closed form to every other mode; its accumulator lives in
-  // C in the band's compact layout (kt <= N/2 + 1, i.e. N >= 16, keeps that inside C)
-  const int band_rk = lin_ok && c.step_form >= 2 && c.kt <= c.h;
   for (int st = 0; st < nsteps; ++st) {
-    for (int rk = 0; rk < 4; ++rk) {
-      EpiParams prm;
-      prm.a_dt = (float)(a_rk4[rk] * d.dt);
-      prm.b_dt = rk < 3 ? (float)(b_rk4[rk] * d.dt) : 0.f;
-      prm.nu = (float)d.nu;
-      prm.drag = (float)d.drag;
-      prm.kolm_amp = (float)d.kolm_amp;
-      prm.kolm_k = d.kolm_k;
-      prm.band_kf2 = d.forcing == L3ES_FORCING_CONST_POWER ? d.kf * d.kf : 0;
-      prm.rk = rk;
-      prm.if_h = d.scheme == L3ES_SCHEME_INTEGRATING_FACTOR ? (float)d.dt : 0.f;
-      prm.dt = (float)d.dt;
-      prm.lin = lin_ok;
-      prm.band_rk = band_rk;
-      if (band_rk)
-        plan->tab.stage(c, S, S, S, rk, prm, s);
-      else
-        plan->tab.stage(c, rk == 0 ? S : c.Tb, S, c.Tb, rk, prm, s);
-    }
+    rk4_stages(plan, S, s);
     double* einj = e_inj_dev ? e_inj_dev + (long long)st * c.batch : c.einj;
     double* ke_final = (ke_dev && st == nsteps - 1) ? ke_dev : nullptr;
     // energy partials of the new state by the row-wise float-float pass (a separate

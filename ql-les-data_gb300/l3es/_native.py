@@ -339,8 +339,8 @@ class Plan:
     def step_form(self) -> int:
         """Form of the explicit RK4 step (l3es_plan_get_step_form): 0 one elementwise
         update of the whole spectrum per stage, 1 the closed form of the linear decay
-        outside the dealiased rows, 2 (default) the stage combination fused into the band
-        pass. All forms compute the reference's RK4 step."""
+        outside the dealiased rows, 2 the stage combination fused into the band pass
+        (plans start at 2 in 3D, 1 in 2D). All forms compute the reference's RK4 step."""
         v = ctypes.c_int32()
         _check(self._lib.l3es_plan_get_step_form(self._h, ctypes.byref(v)), "l3es_plan_get_step_form")
         return int(v.value)
