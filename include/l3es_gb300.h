@@ -102,7 +102,8 @@ int64_t l3es_plan_workspace_bytes(const l3es_plan* plan);
 
 /* Kernel schedule of the plan's step (no counterpart in the reference, whose XLA
  * compiler picks its own kernels, spectral_solver.py:130-153): four choices,
- *   [0] 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA),
+ *   [0] 3D: x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA);
+ *       2D: the step's x passes in 2-column tiles (else 8 columns per CTA),
  *   [1] y passes with the radix-8 schedule (else radix 16 from N = 128),
  *   [2] the half-axis line pass: 1 two-for-one for 64 <= N <= 256, 2 two-for-one with
  *       radix-16 line FFTs, 3 the same fed by bulk copies (2 and 3: N = 256 only),

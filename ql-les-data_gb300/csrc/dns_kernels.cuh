@@ -159,7 +159,7 @@ __device__ __forceinline__ void xlin_scale(float2 (&a)[3][Fft<N>::E], int t, int
 // SKIPWX (3D RHS): field 3 (curl_x) is neither transformed nor stored, and fields 1, 2
 // (u_y, u_z) go to the side buffer wx + wxofs (two fields) instead; the y pass
 // (ky_inv_rhs) forms curl_x from them and writes all six fields.
-template <int N, int DIM, bool CURL, bool SKIPWX = false>
+template <int N, int DIM, bool CURL, bool SKIPWX = false, int XW = TW>
 __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, int m, bool ok, float2* sm,
                                               float2* __restrict__ w, long long wofs, long long fs,
                                               const float2* __restrict__ tw, float2* __restrict__ wx = nullptr,
@@ -192,7 +192,7 @@ __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, 
         v[e] = mul_i<kInv>(cr);  // times 1j
       }
     }
-    block_fft<N, E, kInv, TW>(v, sm, t, tw, 1);
+    block_fft<N, E, kInv, XW>(v, sm, t, tw, 1);
     if (ok) {
       float2* dst = (SKIPWX && (f == 1 || f == 2)) ? wx + wxofs + (f - 1) * fs : w + wofs + f * fs;
 #pragma unroll
@@ -202,9 +202,10 @@ __device__ __forceinline__ void kx_inv_fields(float2 (&a)[3][Fft<N>::E], int t, 
   }
 }
 
-// LINF: the x inverse of a band-fused RK stage (XLin).
-template <int N, int DIM, bool CURL, bool SKIPWX = false, bool LINF = false>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
+// LINF: the x inverse of a band-fused RK stage (XLin). XW: columns per CTA (2D grids
+// take narrow tiles: one 256^2 field has only 129 columns).
+template <int N, int DIM, bool CURL, bool SKIPWX = false, bool LINF = false, int XW = TW>
+__global__ void __launch_bounds__(XW * Fft<N>::T)
 kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long long fs,
        const float2* __restrict__ tw, float2* __restrict__ wx = nullptr, XLin xl = XLin{},
        int* __restrict__ err = nullptr) {
@@ -212,9 +213,9 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
   constexpr int NMID = DIM == 3 ? N : 1;
   constexpr int MC = NMID * H;
   constexpr int NF = CURL ? 6 : 3;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
-  const int m = blockIdx.x * TW + p;
+  __shared__ float2 sm[xpad_len<XW>(N) * XW];
+  const int p = threadIdx.x % XW, t = threadIdx.x / XW;
+  const int m = blockIdx.x * XW + p;
   const bool ok = m < MC;
   const long long bofs = (long long)blockIdx.y * 3 * cs;  // batch of trajectories
   if constexpr (LINF) {
@@ -231,8 +232,8 @@ kx_inv(const float2* __restrict__ uh, long long cs, float2* __restrict__ w, long
   if constexpr (LINF) {
     if (ok && xl.rk > 0) xlin_scale<N, DIM>(a, t, m, xl, (int)blockIdx.y, err);
   }
-  kx_inv_fields<N, DIM, CURL, SKIPWX>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw, wx,
-                                      (long long)blockIdx.y * 2 * fs);
+  kx_inv_fields<N, DIM, CURL, SKIPWX, XW>(a, t, m, ok, sm + p, w, (long long)blockIdx.y * NF * fs, fs, tw, wx,
+                                          (long long)blockIdx.y * 2 * fs);
 }
 
 // Persistent 3D variant: each CTA walks the tiles blockIdx.x, + gridDim.x, ...; the
@@ -1339,7 +1340,7 @@ struct BandRk {
 // ------------------------------------------------------------------------------
 // One tile of kx_fwd_band: d[c][e] = DU component c at x row t + T e of column kh of
 // middle row kmb (band index); x forward FFT, dealias mask, Leray projection into P.
-template <int N, int DIM, bool FUSED = false>
+template <int N, int DIM, bool FUSED = false, int XW = TW>
 __device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int t, int kh, int kmb, int kd, int kt,
                                                  float2* sm, float2* __restrict__ P, long long pcs, long long bp,
                                                  const float2* __restrict__ tw, const BandRk* br = nullptr,
@@ -1351,7 +1352,7 @@ __device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int 
   const int mid = km < 0 ? km + N : km;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    block_fft<N, E, kFwd, TW>(d[c], sm, t, tw, 1);
+    block_fft<N, E, kFwd, XW>(d[c], sm, t, tw, 1);
     __syncthreads();
   }
   // (kt can exceed the half axis only at N = 8: those columns hold no mode of S)
@@ -1438,19 +1439,19 @@ __device__ __forceinline__ void kx_fwd_band_tile(float2 (&d)[3][Fft<N>::E], int 
 
 // FUSED: the band-fused RK step (BandRk; the constant-power coefficient then comes from
 // the stage's x inverse, band_kf = 0 here).
-template <int N, int DIM, bool FUSED = false>
-__global__ void __launch_bounds__(TW * Fft<N>::T)
+template <int N, int DIM, bool FUSED = false, int XW = TW>
+__global__ void __launch_bounds__(XW * Fft<N>::T)
 kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2* __restrict__ P, long long pcs,
             const float2* __restrict__ tw, const float2* __restrict__ us, long long cs, int band_kf,
             double inv_n2d, double eps_inj, double* __restrict__ band_scale, const BandRk br = BandRk{}) {
   constexpr int E = Fft<N>::E, T = Fft<N>::T;
   constexpr int NMID = DIM == 3 ? N : 1;
-  __shared__ float2 sm[xpad_len<TW>(N) * TW];
-  const int p = threadIdx.x % TW, t = threadIdx.x / TW;
+  __shared__ float2 sm[xpad_len<XW>(N) * XW];
+  const int p = threadIdx.x % XW, t = threadIdx.x / XW;
   const int kmb = DIM == 3 ? (int)blockIdx.y : 0;
   const int km = DIM == 3 ? kmb - kd : 0;
   const int mid = km < 0 ? km + N : km;
-  const int kh = blockIdx.x * TW + p;  // < kt (kt is a multiple of TW)
+  const int kh = blockIdx.x * XW + p;  // < kt (kt is a multiple of TW, hence of XW)
   const int batch = blockIdx.z;
   const long long bd = (long long)batch * 3 * dcs, bp = (long long)batch * 3 * pcs;
   if (band_kf > 0 && blockIdx.x == 0 && blockIdx.y == 0)
@@ -1461,7 +1462,7 @@ kx_fwd_band(const float2* __restrict__ du, long long dcs, int kt, int kd, float2
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int e = 0; e < E; ++e) d[c][e] = du[bd + c * dcs + ((long long)(t + T * e) * NMID + mid) * kt + kh];
-  kx_fwd_band_tile<N, DIM, FUSED>(d, t, kh, kmb, kd, kt, sm + p, P, pcs, bp, tw, &br, batch);
+  kx_fwd_band_tile<N, DIM, FUSED, XW>(d, t, kh, kmb, kd, kt, sm + p, P, pcs, bp, tw, &br, batch);
 }
 
 // Persistent 3D variant of kx_fwd_band: tiles (column tile, band row kmb) are walked

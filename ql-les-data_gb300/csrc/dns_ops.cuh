@@ -11,6 +11,10 @@ template <int N>
 struct DnsOps {
   static constexpr int H = N / 2 + 1;
   static constexpr int TX = TW * Fft<N>::T;  // threads of the strided x passes
+  // 2D x passes in narrow tiles (schedule entry [0] in 2D): XN columns per CTA, so a
+  // 256^2 field's 129 columns spread over 65 CTAs instead of 17
+  static constexpr int XN = 2;
+  static constexpr int TXN = XN * Fft<N>::T;
   using L = LineCfg<N>;
   using KY = KyCfg<N>;
   static constexpr unsigned ky_tiles(int ncols) { return (unsigned)((ncols + KY::TWY - 1) / KY::TWY); }
@@ -100,6 +104,20 @@ struct DnsOps {
           L3ES_LAUNCH(c, KK_X_INV, bytes, s,
                       kx_inv_tma<N, true, true><<<dim3(gx, c.batch), TX, KxTma<N>::SMEM, s>>>(
                           map, c.W, c.fs, c.tw, ntiles, c.err, c.Wx, XLin{}));
+        return;
+      }
+    }
+    if constexpr (DIM == 2) {
+      if (c.sched.x_bulk) {
+        const dim3 gn((unsigned)((mc + XN - 1) / XN), c.batch);
+        if (xl)
+          L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                      kx_inv<N, 2, true, false, true, XN><<<gn, TXN, 0, s>>>(us, c.cs, c.W, c.fs, c.tw, c.Wx, *xl,
+                                                                            c.err));
+        else
+          L3ES_LAUNCH(c, KK_X_INV, bytes, s,
+                      kx_inv<N, 2, true, false, false, XN><<<gn, TXN, 0, s>>>(us, c.cs, c.W, c.fs, c.tw, c.Wx,
+                                                                             XLin{}, c.err));
         return;
       }
     }
@@ -206,9 +224,14 @@ struct DnsOps {
           return;
         }
       }
-      L3ES_LAUNCH(c, KK_X_EPI, bb, s,
-                  kx_fwd_band<N, DIM, true><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
-                      c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, 0, inv_n2d, c.eps_inj, c.band, br));
+      if (DIM == 2 && c.sched.x_bulk)
+        L3ES_LAUNCH(c, KK_X_EPI, bb, s,
+                    kx_fwd_band<N, DIM, true, XN><<<dim3(c.kt / XN, 1, c.batch), TXN, 0, s>>>(
+                        c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, 0, inv_n2d, c.eps_inj, c.band, br));
+      else
+        L3ES_LAUNCH(c, KK_X_EPI, bb, s,
+                    kx_fwd_band<N, DIM, true><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
+                        c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, 0, inv_n2d, c.eps_inj, c.band, br));
       return;
     }
     // (block 0 of each trajectory also computes the constant-power coefficient of us)
@@ -231,7 +254,12 @@ struct DnsOps {
         band_done = true;
       }
     }
-    if (!band_done)
+    if (!band_done && DIM == 2 && c.sched.x_bulk)
+      L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
+                  kx_fwd_band<N, DIM, false, XN><<<dim3(c.kt / XN, 1, c.batch), TXN, 0, s>>>(
+                      c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,
+                      c.eps_inj, c.band));
+    else if (!band_done)
       L3ES_LAUNCH(c, KK_X_EPI, Adu * rows + Ap, s,
                   kx_fwd_band<N, DIM><<<dim3(c.kt / TW, DIM == 3 ? nb : 1, c.batch), TX, 0, s>>>(
                       c.DU, c.ds, c.kt, c.kd, c.P, c.pcs, c.tw, us, c.cs, prm.band_kf2 > 0 ? c.kf : 0, inv_n2d,

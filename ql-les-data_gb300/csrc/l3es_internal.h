@@ -121,7 +121,8 @@ inline bool misaligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p)
 // Kernel variants of one plan's step (chosen by l3es_plan_autotune; the defaults are the
 // measured best at 256^3 on GB300).
 struct Schedule {
-  int x_bulk = 1;     // 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA)
+  int x_bulk = 1;     // 3D x passes by the persistent bulk-tensor-copy kernels (else one tile per CTA);
+                      // 2D: the step's x passes in 2-column tiles (else 8)
   int y_var = 0;      // y-pass schedule: KyCfg variant (0: radix 16 from N = 128, 1: radix 8)
   int line_pair = 1;  // line pass: 1 two-for-one (64 <= N <= 256), 2 two-for-one radix 16 and 3 the same
                       // fed by bulk copies (N = 256; 3 is its default), 0 packed

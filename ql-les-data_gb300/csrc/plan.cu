@@ -569,7 +569,7 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
     l3es_plan_set_schedule(plan, v);
     // knobs that change anything for this plan
     const int n = c.n;
-    const bool knob[4] = {c.dim == 3 && n >= 64, c.dim == 3 && n >= 128, n >= 64 && n <= 256,
+    const bool knob[4] = {(c.dim == 3 && n >= 64) || c.dim == 2, c.dim == 3 && n >= 128, n >= 64 && n <= 256,
                           c.dim == 3 && n >= 64};
     const int nval[4] = {2, 2, n == 256 ? 4 : 2, 2};  // the line pass has two radix-16 forms at 256
     float best = time_step(plan, s, e0, e1);
