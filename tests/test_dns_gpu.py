@@ -551,6 +551,36 @@ def test_rk_step_forms_agree(case):
         p.step_form = 3
 
 
+@pytest.mark.parametrize("n,batch", [(256, 1), (128, 3), (512, 1)])
+def test_2d_x_tile_widths_agree(n, batch):
+    """2D x passes in 2-column tiles (schedule entry 0, the default in 2D) and in
+    8-column tiles give the same Kolmogorov steps in both 2D step forms, single and
+    batched, and match the FP64 oracle."""
+    nu, dt, steps = 1e-3, 1e-3, 3
+    us = [R.init_u_random2d(n, 11 + b) for b in range(batch)]
+    uh0 = np.stack([np.fft.rfftn(u, axes=(1, 2)).squeeze() for u in us])
+    p = _plan(dim=2, n=n, nu=nu, dt=dt, drag=0.1, kolm_k=4, kolm_amp=1.0, batch=batch)
+    assert p.schedule["x_bulk"] == 1
+    outs = {}
+    for xb in (1, 0):
+        for form in (1, 2):
+            p.set_schedule({"x_bulk": xb})
+            p.step_form = form
+            g = _c64(uh0 if batch > 1 else uh0[0])
+            p.step(g, steps)
+            p.check()
+            outs[(xb, form)] = g.cpu().numpy().reshape(uh0.shape)
+    for key, v in outs.items():
+        assert _rel(v, outs[(1, 1)]) < 2e-6, key
+    rhs = R.rhs_wrapper(n, nu, (1, 2), drag=0.1, force_hat=R.kolmogorov_forcing_hat(n, 1.0, 4))
+    step = R.rk4_wrapper(dt, rhs, None, 0.0, "none", (1, 2))
+    for b in range(batch):
+        uu, uh = us[b], uh0[b]
+        for _ in range(steps):
+            uu, uh, _ = step(uu, uh)
+        assert _rel(outs[(1, 1)][b], uh) < 2e-5
+
+
 def test_line_pass_variants_agree_in_2d_at_256():
     """2D Kolmogorov flow at 256^2 (drag, sin 4y forcing): every line pass variant gives
     the same steps, and the radix-16 forms against the FP64 oracle."""
