@@ -322,7 +322,8 @@ class Plan:
     @property
     def schedule(self) -> dict:
         """The plan's kernel schedule (l3es_plan_get_schedule) as {name: 0 or 1}; line_pair
-        is 2 or 3 for the radix-16 line passes (N = 256; 3 fed by bulk copies)."""
+        is 2 or 3 for the radix-16 line passes (N = 256; 3 fed by bulk copies); x_bulk
+        selects the bulk-copy x passes in 3D and 2-column x-pass tiles in 2D."""
         v = (ctypes.c_int32 * 4)()
         _check(self._lib.l3es_plan_get_schedule(self._h, v), "l3es_plan_get_schedule")
         return dict(zip(self.SCHEDULE_KEYS, list(v)))
