@@ -581,6 +581,28 @@ def test_2d_x_tile_widths_agree(n, batch):
         assert _rel(outs[(1, 1)][b], uh) < 2e-5
 
 
+def test_forcing_outside_the_band_takes_the_whole_spectrum_form():
+    """Constant-power forcing on shells beyond the dealiased band (kf = 7 > kd = 5 at
+    16^3) puts a forcing term on modes the band pass does not own: every step form then
+    runs the whole-spectrum update, and the step matches the FP64 oracle."""
+    n, nu, dt, kf, eps = 16, 5e-3, 2e-3, 7, 0.1
+    u0 = R.init_u_hit(n, 5, spectrum="k4exp", kp=3.0)
+    uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
+    _, kkk2, _, _ = R.wavenumbers(n, 3)
+    mask = ((kkk2 > 0) & (kkk2 <= kf * kf)).astype(float)
+    step = R.rk4_wrapper(dt, R.rhs_wrapper(n, nu, const_power=(eps, mask)), None, 0.0, "none")
+    uu, uh = u0, uh0
+    for _ in range(3):
+        uu, uh, _ = step(uu, uh)
+    p = _plan(dim=3, n=n, nu=nu, dt=dt, forcing="const_power", kf=kf, eps_inj=eps)
+    for form in (2, 1, 0):
+        p.step_form = form
+        g = _c64(uh0)
+        p.step(g, 3)
+        p.check()
+        assert _rel(g.cpu().numpy(), uh) < RTOL, form
+
+
 def test_line_pass_variants_agree_in_2d_at_256():
     """2D Kolmogorov flow at 256^2 (drag, sin 4y forcing): every line pass variant gives
     the same steps, and the radix-16 forms against the FP64 oracle."""
