@@ -560,7 +560,14 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
   Ctx& c = plan->ctx;
   KTimer* timer = c.timer;
   c.timer = nullptr;  // untimed by the per-kernel timer
-  rc = cuda_check(cudaMemsetAsync(c.Tb, 0, sizeof(float2) * 3 * c.cs * c.batch, s), "l3es_plan_autotune memset");
+  // the timed steps run on scratch; whatever they flag in the error word (a constant-power
+  // coefficient of a zero field can overflow) is not the caller's: keep the word as it was
+  int err_word = 0;
+  rc = cuda_check(cudaMemcpyAsync(&err_word, c.err, sizeof(int), cudaMemcpyDeviceToHost, s),
+                  "l3es_plan_autotune error word");
+  if (rc == L3ES_OK) rc = cuda_check(cudaStreamSynchronize(s), "l3es_plan_autotune sync");
+  if (rc == L3ES_OK)
+    rc = cuda_check(cudaMemsetAsync(c.Tb, 0, sizeof(float2) * 3 * c.cs * c.batch, s), "l3es_plan_autotune memset");
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (rc == L3ES_OK) rc = cuda_check(cudaEventCreate(&e0), "l3es_plan_autotune event");
   if (rc == L3ES_OK) rc = cuda_check(cudaEventCreate(&e1), "l3es_plan_autotune event");
@@ -596,7 +603,10 @@ extern "C" int l3es_plan_autotune(l3es_plan* plan, const char* cache_path, void*
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   c.timer = timer;
-  return rc;
+  const int rc2 = cuda_check(cudaMemcpyAsync(c.err, &err_word, sizeof(int), cudaMemcpyHostToDevice, s),
+                             "l3es_plan_autotune error word");
+  const int rc3 = cuda_check(cudaStreamSynchronize(s), "l3es_plan_autotune sync");
+  return rc != L3ES_OK ? rc : rc2 != L3ES_OK ? rc2 : rc3;
 }
 
 // per-block partial sums of w |u_hat|^2 into c.partial ([batch][nblk]); returns nblk

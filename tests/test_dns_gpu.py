@@ -640,3 +640,8 @@ def test_autotune_picks_a_schedule_and_caches_it(tmp_path):
     q.set_schedule({k: 1 - v for k, v in s1.items()})
     assert q.autotune(cache) == s1  # read from the cache, not re-timed
     assert len(open(cache).read().splitlines()) == 1
+    # the tuner times whole steps on zeroed scratch, where a constant-power coefficient
+    # can overflow: nothing of that reaches the plan's error word
+    r = _plan(dim=2, n=64, nu=1e-3, dt=1e-3, forcing="const_power", kf=2, eps_inj=0.1, kolm_k=4, kolm_amp=1.0)
+    r.autotune("")
+    r.check()
