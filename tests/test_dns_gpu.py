@@ -582,23 +582,23 @@ def test_2d_x_tile_widths_agree(n, batch):
 
 
 def test_forcing_outside_the_band_takes_the_whole_spectrum_form():
-    """Constant-power forcing on shells beyond the dealiased band (kf = 7 > kd = 5 at
-    16^3) puts a forcing term on modes the band pass does not own: every step form then
-    runs the whole-spectrum update, and the step matches the FP64 oracle."""
-    n, nu, dt, kf, eps = 16, 5e-3, 2e-3, 7, 0.1
-    u0 = R.init_u_hit(n, 5, spectrum="k4exp", kp=3.0)
-    uh0 = np.fft.rfftn(u0, axes=(1, 2, 3))
-    _, kkk2, _, _ = R.wavenumbers(n, 3)
-    mask = ((kkk2 > 0) & (kkk2 <= kf * kf)).astype(float)
-    step = R.rk4_wrapper(dt, R.rhs_wrapper(n, nu, const_power=(eps, mask)), None, 0.0, "none")
-    uu, uh = u0, uh0
-    for _ in range(3):
+    """A Kolmogorov forcing wavenumber beyond the stored band (kolm_k = 26 >= kt = 24 at
+    64^2) puts a forcing term on a mode the band pass does not own: every requested step
+    form then runs the whole-spectrum update, and the steps match the FP64 oracle.
+    (Constant-power forcing cannot reach beyond the band: plans take kf <= N/4 < kd.)"""
+    n, nu, dt, kk, steps = 64, 1e-3, 1e-3, 26, 3
+    u = R.init_u_random2d(n, 11)
+    uh0 = np.fft.rfftn(u, axes=(1, 2)).squeeze()
+    rhs = R.rhs_wrapper(n, nu, (1, 2), drag=0.1, force_hat=R.kolmogorov_forcing_hat(n, 1.0, kk))
+    step = R.rk4_wrapper(dt, rhs, None, 0.0, "none", (1, 2))
+    uu, uh = u, uh0
+    for _ in range(steps):
         uu, uh, _ = step(uu, uh)
-    p = _plan(dim=3, n=n, nu=nu, dt=dt, forcing="const_power", kf=kf, eps_inj=eps)
+    p = _plan(dim=2, n=n, nu=nu, dt=dt, drag=0.1, kolm_k=kk, kolm_amp=1.0)
     for form in (2, 1, 0):
         p.step_form = form
         g = _c64(uh0)
-        p.step(g, 3)
+        p.step(g, steps)
         p.check()
         assert _rel(g.cpu().numpy(), uh) < RTOL, form
 
