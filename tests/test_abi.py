@@ -50,6 +50,14 @@ def test_invalid_arguments_fail_without_gpu():
     assert b"not supported" in lib.l3es_last_error()
     assert lib.l3es_step(None, None, None, 1, None, None) == -1
     assert lib.l3es_plan_check(None) == -1
+    form = ctypes.c_int32()
+    assert lib.l3es_plan_get_step_form(None, ctypes.byref(form)) == -1
+    assert b"null" in lib.l3es_last_error()
+    assert lib.l3es_plan_set_step_form(None, 1) == -1
+    assert b"step_form" in lib.l3es_last_error()
+    sched = (ctypes.c_int32 * 4)()
+    assert lib.l3es_plan_get_schedule(None, sched) == -1
+    assert lib.l3es_plan_autotune(None, None, None) == -1
 
 
 def test_header_is_plain_c99(tmp_path):
