@@ -509,7 +509,8 @@ def test_every_kernel_schedule_gives_the_same_step(n):
 
 
 @pytest.mark.parametrize("case", ["3d64_const_power", "3d128_none", "3d64_const_power_batch3_x_plain",
-                                  "2d256_kolmogorov", "3d256_const_power"])
+                                  "2d256_kolmogorov", "3d256_const_power", "3d64_drag_nu_batch2",
+                                  "3d32_ekin_tot"])
 def test_rk_step_forms_agree(case):
     """The three forms of the explicit RK4 step (one elementwise update of the whole
     spectrum; the closed form of the linear decay outside the dealiased rows; the stage
@@ -534,7 +535,16 @@ def test_rk_step_forms_agree(case):
         kw = dict(dim=3, n=n, nu=5e-3, dt=2e-3)
         if "const_power" in case:
             kw.update(forcing="const_power", kf=2, eps_inj=0.1)
+        if "drag" in case:
+            kw.update(drag=0.05)
+        if "ekin_tot" in case:
+            kw.update(forcing="ekin_tot", kf=2, e_kin_init=0.5)
+    if "batch2" in case:  # the drag case also runs two trajectories of different viscosity
+        batch = 2
+        uh0 = np.stack([uh0[0], 0.5 * uh0[0]])
     p = _plan(batch=batch, **kw)
+    if "nu" in case.split("_"):
+        p.set_nu([5e-3, 2e-2])
     assert p.step_form == (2 if kw["dim"] == 3 else 1)
     if "x_plain" in case:
         p.set_schedule({"x_bulk": 0, "band_bulk": 0})
