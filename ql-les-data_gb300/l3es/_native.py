@@ -223,7 +223,7 @@ class Plan:
     def step(self, u_hat, nsteps: int = 1, u_out=None, e_inj=None, ke=None, stream=None) -> None:
         """In-place RK4 steps on u_hat (optionally irfftn into u_out at the end). ke: a
         float64 device tensor of `batch` values that receives the kinetic energy of the
-        final state (taken from the last stage's energy sums, no extra pass)."""
+        final state (one float-float energy pass over it, inside the same call)."""
         self._check_spec(u_hat)
         if u_out is not None:
             self._check_phys(u_out)
