@@ -1217,9 +1217,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_GRID)
-    ap.add_argument("--workload", default="hit256", choices=["hit256", "batch24", "adjoint"],
+    ap.add_argument("--workload", default="hit256", choices=["hit256", "batch24", "adjoint", "kolm2d"],
                     help="hit256: the metric's 256^3 step; batch24: 24 mixed trajectories; "
-                         "adjoint: the 128^3 differentiation workload alone")
+                         "adjoint: the 128^3 differentiation workload alone; kolm2d: the 2D Kolmogorov "
+                         "256^2 configuration alone (its --steps steps, at least 1000)")
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--ke-steps", type=int, default=1000,
                     help="steps of the FP32-vs-FP64 accuracy check: kinetic energy (the metric's clause), "
@@ -1253,6 +1254,9 @@ def main():
         return run_reference(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "kolm2d":
+        print(json.dumps(kolm2d_rate(args.steps, args.warmup)), flush=True)
+        return 0
     return run_batch24(args) if args.workload == "batch24" else run_ours(args)
 
 
